@@ -1,0 +1,269 @@
+"""fyfft_gb300 -- GB300-native (sm_103a) 1D complex FFT with fyFFT's plan/execute interface.
+
+The Python surface mirrors the reference's C++ class ``fy::fft::FFT1D_C2C_invoker``
+(foye_FFT.hpp:89-185):
+
+    inv = FFT1D_C2C_invoker(N)                   # plan (strategy, tables, scratch) once
+    inv.dispatch(False, x, y)                   # forward  exp(-2 pi i kn/N)
+    inv.dispatch(True, x, y)                    # inverse  exp(+2 pi i kn/N) / N
+    FFT1D_C2C_invoker.acquired_execution_strategy(N)   # the reference's strategy for N
+
+and adds batching, complex128, an adjoint entry point and an uneven-length batch.  Every call
+goes through the C ABI of libfygpu.so (include/fygpu.h) into hand-written CUDA kernels; there
+is no CPU fallback: without the built library (``fyfft_gb300.build.build()``) importing the
+ABI raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+import os
+
+import numpy as np
+
+from . import build as _build_mod
+
+LIB_PATH = _build_mod.LIB
+
+FYG_OK = 0
+FYG_C32, FYG_C64 = 0, 1
+FYG_FORWARD, FYG_INVERSE = 1, -1
+FYG_FLAG_CONV_FP64, FYG_FLAG_CONV_FP32, FYG_FLAG_NO_L2_CHUNK = 1, 2, 4
+
+# every symbol include/fygpu.h declares
+EXPORTED_SYMBOLS = (
+    "fyg_plan_create", "fyg_plan_destroy", "fyg_execute", "fyg_execute_adjoint", "fyg_strategy",
+    "fyg_gpu_strategy", "fyg_plan_info", "fyg_batch_create", "fyg_batch_destroy",
+    "fyg_batch_execute", "fyg_batch_execute_plain", "fyg_last_error_string", "fyg_fill_random",
+    "fyg_fill_random_device", "fyg_version",
+)
+
+
+class FFT_execution_strategy(enum.IntEnum):
+    """foye_FFT.hpp:153-160"""
+    kernel_direct = 0
+    mix_radix = 1
+    rader = 2
+    bluestein = 3
+    DFT = 4
+
+
+class FygError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"fygpu error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded libfygpu.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with fyfft_gb300.build.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        sz, vp, i, d, u64 = ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_uint64
+        L.fyg_plan_create.argtypes = [sz, i, sz, i, ctypes.POINTER(vp)]
+        L.fyg_plan_destroy.argtypes = [vp]
+        L.fyg_execute.argtypes = [vp, vp, vp, i, vp]
+        L.fyg_execute_adjoint.argtypes = [vp, vp, vp, d, vp]
+        L.fyg_strategy.argtypes = [sz]
+        L.fyg_gpu_strategy.argtypes = [sz]
+        L.fyg_plan_info.argtypes = [vp, ctypes.POINTER(sz), ctypes.POINTER(i), ctypes.POINTER(i)]
+        L.fyg_batch_create.argtypes = [ctypes.POINTER(sz), sz, i, i, ctypes.POINTER(vp)]
+        L.fyg_batch_destroy.argtypes = [vp]
+        L.fyg_batch_execute.argtypes = [vp, vp, vp, vp, i, vp]
+        L.fyg_batch_execute_plain.argtypes = [vp, vp, vp, i, vp]
+        L.fyg_last_error_string.restype = ctypes.c_char_p
+        L.fyg_fill_random.argtypes = [u64, i, i, sz, vp]
+        L.fyg_fill_random_device.argtypes = [u64, i, i, sz, vp, vp]
+        L.fyg_version.restype = ctypes.c_char_p
+        _lib = L
+    return _lib
+
+
+def check(rc: int) -> None:
+    if rc != FYG_OK:
+        raise FygError(rc, lib().fyg_last_error_string().decode())
+
+
+def _stream_handle(stream) -> int | None:
+    if stream is None:
+        try:
+            import torch
+            if torch.cuda.is_available():
+                return torch.cuda.current_stream().cuda_stream
+        except ImportError:
+            pass
+        return None
+    return getattr(stream, "cuda_stream", stream)
+
+
+def _buffer_ptr(x):
+    """(pointer, n_complex, dtype code, on_device) of a torch tensor or numpy array."""
+    if isinstance(x, np.ndarray):
+        if not x.flags.c_contiguous:
+            raise ValueError("arrays must be C-contiguous")
+        if x.dtype == np.complex64:
+            return x.ctypes.data, x.size, FYG_C32, False
+        if x.dtype == np.complex128:
+            return x.ctypes.data, x.size, FYG_C64, False
+        if x.dtype == np.float32:
+            return x.ctypes.data, x.size // 2, FYG_C32, False
+        if x.dtype == np.float64:
+            return x.ctypes.data, x.size // 2, FYG_C64, False
+        raise TypeError(f"unsupported dtype {x.dtype}")
+    import torch
+    if not x.is_contiguous():
+        raise ValueError("tensors must be contiguous")
+    dt = {torch.complex64: (FYG_C32, 1), torch.complex128: (FYG_C64, 1),
+          torch.float32: (FYG_C32, 2), torch.float64: (FYG_C64, 2)}.get(x.dtype)
+    if dt is None:
+        raise TypeError(f"unsupported dtype {x.dtype}")
+    return x.data_ptr(), x.numel() // dt[1], dt[0], x.is_cuda
+
+
+def fill_random(seed: int, n_complex: int, dtype=np.complex64, dist: str = "uniform") -> np.ndarray:
+    """Seeded synthetic data on the host (uniform re/im in [-1, 1) or standard normal)."""
+    out = np.empty(n_complex, dtype=dtype)
+    code = FYG_C32 if np.dtype(dtype) == np.complex64 else FYG_C64
+    check(lib().fyg_fill_random(seed, 0 if dist == "uniform" else 1, code, n_complex, out.ctypes.data))
+    return out
+
+
+def fill_random_device(seed: int, out, dist: str = "uniform", stream=None) -> None:
+    """Same stream as fill_random, generated on the GPU into a CUDA tensor."""
+    ptr, n, code, _ = _buffer_ptr(out)
+    check(lib().fyg_fill_random_device(seed, 0 if dist == "uniform" else 1, code, n, ptr,
+                                       _stream_handle(stream)))
+
+
+class FFT1D_C2C_invoker:
+    """GPU plan for `batch` contiguous transforms of length N (foye_FFT.hpp:89-185).
+
+    dtype: "complex64" (the reference's float buffers) or "complex128".
+    """
+
+    FFT_execution_strategy = FFT_execution_strategy
+
+    def __init__(self, length: int, dtype="complex64", batch: int = 1, flags: int = 0):
+        self.N = int(length)
+        self.batch = int(batch)
+        self.dtype_code = FYG_C32 if str(dtype).endswith("complex64") else FYG_C64
+        h = ctypes.c_void_p()
+        check(lib().fyg_plan_create(self.N, self.dtype_code, self.batch, flags, ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fyg_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _io(self, x, y):
+        px, nx, dx, _ = _buffer_ptr(x)
+        py, ny, dy, _ = _buffer_ptr(y)
+        need = self.N * self.batch
+        if dx != self.dtype_code or dy != self.dtype_code:
+            raise TypeError("buffer dtype does not match the plan")
+        if nx < need or ny < need:
+            raise ValueError(f"buffers hold {nx}/{ny} complex elements, plan needs {need}")
+        return px, py
+
+    def dispatch(self, invert: bool, input, output, stream=None) -> None:
+        """foye_FFT.hpp:128-151: dispatch<invert>(input, output)."""
+        px, py = self._io(input, output)
+        check(lib().fyg_execute(self._h, px, py, FYG_INVERSE if invert else FYG_FORWARD,
+                                _stream_handle(stream)))
+
+    def forward(self, input, output, stream=None) -> None:
+        self.dispatch(False, input, output, stream)
+
+    def backward(self, input, output, stream=None) -> None:
+        self.dispatch(True, input, output, stream)
+
+    def adjoint(self, g, output, scale: float = 1.0, stream=None) -> None:
+        """output = scale * F^H g (= scale * N * backward(g))."""
+        px, py = self._io(g, output)
+        check(lib().fyg_execute_adjoint(self._h, px, py, float(scale), _stream_handle(stream)))
+
+    def info(self):
+        L, P, S = ctypes.c_size_t(), ctypes.c_int(), ctypes.c_int()
+        check(lib().fyg_plan_info(self._h, ctypes.byref(L), ctypes.byref(P), ctypes.byref(S)))
+        return {"conv_length": L.value, "passes": P.value, "gpu_strategy": S.value}
+
+    @staticmethod
+    def acquired_execution_strategy(length: int) -> FFT_execution_strategy:
+        """foye_FFT.hpp:162-184 (the reference's choice, reported unchanged)."""
+        s = lib().fyg_strategy(int(length))
+        if s < 0:
+            raise ValueError("length must be >= 2")
+        return FFT_execution_strategy(s)
+
+    @staticmethod
+    def gpu_execution_strategy(length: int) -> FFT_execution_strategy:
+        """The strategy this library runs (never DFT)."""
+        return FFT_execution_strategy(lib().fyg_gpu_strategy(int(length)))
+
+
+class UnevenBatch:
+    """Many transforms of different lengths packed back to back, run by one persistent kernel."""
+
+    def __init__(self, lengths, dtype="complex64", flags: int = 0):
+        self.lengths = [int(n) for n in lengths]
+        self.dtype_code = FYG_C32 if str(dtype).endswith("complex64") else FYG_C64
+        arr = (ctypes.c_size_t * len(self.lengths))(*self.lengths)
+        h = ctypes.c_void_p()
+        check(lib().fyg_batch_create(arr, len(self.lengths), self.dtype_code, flags, ctypes.byref(h)))
+        self._h = h
+        self.offsets = np.concatenate([[0], np.cumsum(self.lengths)[:-1]]).astype(np.int64)
+        self.total = int(sum(self.lengths))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fyg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def execute(self, x, y, invert: bool = False, offsets_dev=None, stream=None) -> None:
+        px, _, _, _ = _buffer_ptr(x)
+        py, _, _, _ = _buffer_ptr(y)
+        po = None if offsets_dev is None else _buffer_ptr(offsets_dev)[0]
+        check(lib().fyg_batch_execute(self._h, px, py, po, FYG_INVERSE if invert else FYG_FORWARD,
+                                      _stream_handle(stream)))
+
+    def execute_plain(self, x, y, invert: bool = False, stream=None) -> None:
+        px, _, _, _ = _buffer_ptr(x)
+        py, _, _, _ = _buffer_ptr(y)
+        check(lib().fyg_batch_execute_plain(self._h, px, py, FYG_INVERSE if invert else FYG_FORWARD,
+                                            _stream_handle(stream)))
+
+
+_plan_cache: dict = {}
+
+
+def fft(x, inverse: bool = False, stream=None):
+    """Transform along the last axis of a contiguous CUDA tensor (complex64 or complex128)."""
+    import torch
+    n = x.shape[-1]
+    batch = x.numel() // n
+    key = (n, batch, x.dtype, x.device)
+    plan = _plan_cache.get(key)
+    if plan is None:
+        plan = FFT1D_C2C_invoker(n, "complex64" if x.dtype == torch.complex64 else "complex128", batch)
+        _plan_cache[key] = plan
+    y = torch.empty_like(x)
+    plan.dispatch(inverse, x.contiguous(), y, stream)
+    return y

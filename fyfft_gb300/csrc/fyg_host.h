@@ -1,0 +1,88 @@
+// fyg_host.h -- host-side plan structures of the GB300 FFT library.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/fygpu.h"
+#include "fyg_internal.h"
+
+namespace fyg {
+
+int set_error(int code, const std::string& msg);
+void clear_error();
+const char* last_error();
+int cuda_error(cudaError_t e, const char* what);
+void fill_random_host(uint64_t seed, int dist, int dtype, size_t n, void* out);
+
+FastDiv make_fastdiv(uint32_t d);
+
+// GPU-side strategy of a plan (what actually runs).
+enum GpuStrategy : int {
+    GS_SINGLE = 0,      // one tile pass (whole transform in one CTA)
+    GS_MULTI = 1,       // multi-pass Stockham (four-step generalised), fused inter-pass twiddles
+    GS_RADER = 2,       // Rader: cyclic (or zero-padded) convolution of length N-1
+    GS_BLUESTEIN = 3,   // Bluestein chirp-z convolution
+    GS_COPY = 4,        // n == 1
+};
+
+// Owned device allocation.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf();
+    int alloc(size_t n);      // returns FYG_OK / FYG_ERR_ALLOC
+    int upload(const void* host, size_t n);
+};
+
+// Buffer roles a pass reads from / writes to.
+enum Role : int { ROLE_IN = 0, ROLE_OUT = 1, ROLE_S0 = 2, ROLE_S1 = 3 };
+
+struct PassDesc {
+    PassParams p;          // in/out/ncols/x0buf/dcbuf filled at execution
+    int in_role, out_role;
+    int kv;                // kernel variant
+    int threads;
+    size_t smem;
+    int64_t in_elem_bytes, out_elem_bytes;
+};
+
+// In-CTA schedule of a length-R sub-transform.
+struct TilePlan {
+    int R = 0;
+    std::vector<int> radix;
+};
+
+// Per-length tables (w_R for the in-CTA stages; two-level w_L for inter-pass twiddles).
+struct TwiddleSet {
+    DevBuf local_f, local_d;   // keyed per R inside the plan
+};
+
+struct fyg_plan_impl;
+
+}  // namespace fyg
+
+// The opaque plan type of the C ABI.
+struct fyg_plan {
+    size_t n = 0, batch = 0;
+    int dtype = FYG_C32;
+    int flags = 0;
+    int device = 0;
+    int strategy = 0;         // fyg::GpuStrategy
+    int conv_fp64 = 0;        // Rader/Bluestein convolution runs in FP64
+    size_t L = 0;             // algorithm length: n (plain) or the convolution length
+    size_t chunk = 1;         // transforms per chunk (L2-resident scratch)
+    int compute_bytes = 8;    // bytes of one compute complex
+    std::vector<fyg::PassDesc> fwd, inv;
+    // device tables
+    std::vector<std::unique_ptr<fyg::DevBuf>> tables;
+    fyg::DevBuf scratch0, scratch1, x0buf, dcbuf, errword;
+    fyg::DevBuf stage_in, stage_out;   // staging for host pointers
+    size_t stage_in_bytes = 0;
+};

@@ -1,0 +1,40 @@
+// fyg_internal.h -- host-side declarations shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fyg_pass.cuh"
+
+namespace fyg {
+
+// Tile-pass kernel variants: compute type / input type / output type and the launch bound
+// (MAXT threads per CTA).
+enum KernelVariant : int {
+    KV_F32_T1024 = 0,   // float  compute, float  I/O
+    KV_F32_T256,
+    KV_F64_T512,        // double compute, double I/O
+    KV_F64_T256,
+    KV_F64_IF32_T512,   // double compute, float in,  double out
+    KV_F64_OF32_T512,   // double compute, double in, float out
+    KV_F64_F32IO_T512,  // double compute, float in,  float out
+    KV_COUNT
+};
+
+struct VariantInfo { int maxt, compute_bytes; };
+VariantInfo variant_info(int kv);
+
+// Launches one tile pass; sets the dynamic shared-memory attribute when needed.
+cudaError_t launch_pass(int kv, const PassParams& p, unsigned grid, int threads, size_t smem,
+                        cudaStream_t st);
+
+// Uploads the codelet constant tables to the current device (once per device).
+cudaError_t ensure_device_constants();
+
+// Device RNG fill (fyg_fill_random_device).
+cudaError_t launch_fill_random(uint64_t seed, int dist, int dtype, size_t n, void* out,
+                               cudaStream_t st);
+
+// Small helper kernels.
+cudaError_t launch_convert_d2f(const double2* in, float2* out, size_t n, cudaStream_t st);
+
+}  // namespace fyg

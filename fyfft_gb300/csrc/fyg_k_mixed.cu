@@ -1,0 +1,13 @@
+// Tile-pass kernels with FP64 arithmetic on FP32 input and/or output: the FP64 convolution
+// of FP32 Rader/Bluestein plans whose length breaks the FP32 error budget.
+#include "fyg_k_variant.cuh"
+namespace fyg {
+cudaError_t launch_mixed(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st) {
+    if (kv == KV_F64_IF32_T512) return launch_variant<double, float, double, 512>(p, grid, threads, smem, st);
+    if (kv == KV_F64_OF32_T512) return launch_variant<double, double, float, 512>(p, grid, threads, smem, st);
+    return launch_variant<double, float, float, 512>(p, grid, threads, smem, st);
+}
+cudaError_t upload_consts_mixed(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd) {
+    return upload_consts_tu(kf, kd);
+}
+}  // namespace fyg

@@ -1,0 +1,32 @@
+// fyg_k_variant.cuh -- explicit instantiation helper for one tile-pass kernel variant.
+#pragma once
+#include "fyg_internal.h"
+#include "fyg_kernels.cuh"
+
+namespace fyg {
+
+template <typename T, typename TI, typename TO, int MAXT>
+cudaError_t launch_variant(const PassParams& p, unsigned grid, int threads, size_t smem,
+                           cudaStream_t st) {
+    auto kern = k_pass<T, TI, TO, MAXT>;
+    constexpr int kMaxDev = 64;
+    static size_t smem_set[kMaxDev] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (smem > 48 * 1024 && dev < kMaxDev && smem > smem_set[dev]) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        smem_set[dev] = smem;
+    }
+    kern<<<grid, threads, smem, st>>>(p);
+    return cudaGetLastError();
+}
+
+// Copies the codelet constants into this translation unit's __constant__ tables.
+inline cudaError_t upload_consts_tu(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd) {
+    cudaError_t e = cudaMemcpyToSymbol(g_kf, &kf, sizeof(kf));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_kd, &kd, sizeof(kd));
+    return e;
+}
+
+}  // namespace fyg

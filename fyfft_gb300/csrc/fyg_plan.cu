@@ -1,0 +1,870 @@
+// fyg_plan.cu -- planner and executor of the GB300 FFT library, and the plan part of the C ABI.
+//
+// Plan construction replaces fy::fft::FFT1D_C2C_invoker's constructor (foye_FFT.hpp:101-126):
+// the strategy is chosen once, the stage schedule is derived from N's factorization, and all
+// tables (twiddles, chirp, Rader permutations, convolution spectra) are computed once on the
+// host in long double (spectra: FP64 GPU FFT of the long-double kernel) and uploaded.
+//
+// GPU strategies:
+//   single    N <= one CTA's capacity and 13-smooth: one tile pass, several transforms per CTA
+//             (replaces the smooth registry's radix engines and micro-kernels,
+//             src/foye_FFT_radix_wrap.hpp:6-124, src/foye_FFT_radix{2,3,4,5,7}.hpp,
+//             src/foye_FFT_microKernel.hpp, and the batch kernel src/foye_FFT_batch_kernel.hpp)
+//   multi     13-smooth N above that: 2-3 Stockham passes of radix <= ~1800 with the inter-pass
+//             twiddle fused into the next pass's load (replaces the mixed-radix planner and
+//             executor, src/foye_FFT_mix_radix.hpp:253-574)
+//   rader     prime N with 13-smooth N-1: cyclic convolution of length N-1; other primes up to
+//             the reference's Rader limit (39064): zero-padded linear convolution of 7-smooth
+//             length M >= 2N-3 (src/foye_FFT_rader.hpp:142-401)
+//   bluestein everything else: chirp-z with 7-smooth M >= 2N-1 (src/foye_FFT_bluestein.hpp:79-355)
+// The reference's O(N^2) DFT fallback (src/foye_FFT_dft.hpp) is never used.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <mutex>
+
+#include "fyg_host.h"
+
+namespace fyg {
+
+cudaError_t launch_f32(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st);
+cudaError_t launch_f64(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st);
+cudaError_t launch_mixed(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st);
+cudaError_t launch_scale_copy(const void* in, void* out, size_t n, int dtype, double scale, int conj,
+                              cudaStream_t st);
+
+VariantInfo variant_info(int kv) {
+    switch (kv) {
+        case KV_F32_T1024: return {1024, 8};
+        case KV_F32_T256: return {256, 8};
+        case KV_F64_T512: return {512, 16};
+        case KV_F64_T256: return {256, 16};
+        default: return {512, 16};
+    }
+}
+
+cudaError_t launch_pass(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st) {
+    if (kv == KV_F32_T1024 || kv == KV_F32_T256) return launch_f32(kv, p, grid, threads, smem, st);
+    if (kv == KV_F64_T512 || kv == KV_F64_T256) return launch_f64(kv, p, grid, threads, smem, st);
+    return launch_mixed(kv, p, grid, threads, smem, st);
+}
+
+DevBuf::~DevBuf() {
+    if (ptr) cudaFree(ptr);
+}
+
+int DevBuf::alloc(size_t n) {
+    if (ptr) { cudaFree(ptr); ptr = nullptr; bytes = 0; }
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMalloc(&ptr, n);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        cudaGetLastError();
+        return set_error(FYG_ERR_ALLOC, "cudaMalloc(" + std::to_string(n) + ") failed: " + cudaGetErrorString(e));
+    }
+    bytes = n;
+    return FYG_OK;
+}
+
+int DevBuf::upload(const void* host, size_t n) {
+    int rc = alloc(n);
+    if (rc) return rc;
+    cudaError_t e = cudaMemcpy(ptr, host, n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_error(e, "table upload");
+    return FYG_OK;
+}
+
+FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f;
+    f.d = d;
+    uint32_t s = 0;
+    while ((1ull << s) < d) ++s;
+    const uint64_t m = ((1ull << 32) * ((1ull << s) - d)) / d + 1;
+    f.m = (uint32_t)m;
+    f.s = s;
+    return f;
+}
+
+// ------------------------------------------------------------------------------------------
+// Number theory and the reference's strategy chain
+// ------------------------------------------------------------------------------------------
+
+static bool is_prime(uint64_t n) {
+    if (n < 2) return false;
+    if (n < 4) return true;
+    if (n % 2 == 0 || n % 3 == 0) return false;
+    for (uint64_t i = 5; i * i <= n; i += 6)
+        if (n % i == 0 || n % (i + 2) == 0) return false;
+    return true;
+}
+
+static uint64_t mulmod(uint64_t a, uint64_t b, uint64_t m) { return (uint64_t)((unsigned __int128)a * b % m); }
+
+static uint64_t powmod(uint64_t b, uint64_t e, uint64_t m) {
+    uint64_t r = 1 % m;
+    b %= m;
+    while (e) {
+        if (e & 1) r = mulmod(r, b, m);
+        b = mulmod(b, b, m);
+        e >>= 1;
+    }
+    return r;
+}
+
+static uint64_t primitive_root(uint64_t p) {
+    if (p == 2) return 1;
+    std::vector<uint64_t> f;
+    uint64_t m = p - 1;
+    for (uint64_t q = 2; q * q <= m; ++q)
+        if (m % q == 0) { f.push_back(q); while (m % q == 0) m /= q; }
+    if (m > 1) f.push_back(m);
+    for (uint64_t g = 2; g < p; ++g) {
+        bool ok = true;
+        for (uint64_t q : f) if (powmod(g, (p - 1) / q, p) == 1) { ok = false; break; }
+        if (ok) return g;
+    }
+    return 0;
+}
+
+// largest prime factor of n (1 for n == 1)
+static uint64_t max_prime_factor(uint64_t n) {
+    uint64_t best = 1;
+    for (uint64_t q = 2; q * q <= n; ++q)
+        while (n % q == 0) { best = q; n /= q; }
+    if (n > 1) best = std::max(best, n);
+    return best;
+}
+
+static bool is_smooth(uint64_t n, uint64_t b) { return n >= 1 && max_prime_factor(n) <= b; }
+
+static uint64_t next_smooth7(uint64_t n) {
+    for (uint64_t m = std::max<uint64_t>(n, 1);; ++m)
+        if (is_smooth(m, 7)) return m;
+}
+
+// The 38 lengths the reference's smooth registry supports directly (pure powers of 2, 3, 5, 7
+// in its radix engines; src/foye_FFT_radix_wrap.hpp:87-98).  Needed to answer
+// acquired_execution_strategy() exactly as the reference does.
+static bool ref_directly_supported(uint64_t n) {
+    auto pure_power = [](uint64_t n, uint64_t b, uint64_t maxv) {
+        if (n < b || n > maxv) return false;
+        while (n % b == 0) n /= b;
+        return n == 1;
+    };
+    return pure_power(n, 2, 65536) || pure_power(n, 3, 59049) || pure_power(n, 5, 78125) ||
+           pure_power(n, 7, 16807);
+}
+
+// foye_FFT.hpp:162-184 with src/foye_FFT_mix_radix.hpp:618-643 (every 7-smooth length is
+// mixed-radix processable), src/foye_FFT_rader.hpp:403-423 (non-registered prime with
+// 2n-3 <= 78125) and src/foye_FFT_bluestein.hpp:188-215 (n <= 39062).
+static int ref_strategy(uint64_t n) {
+    if (n < 2) return -1;
+    if (ref_directly_supported(n)) return FYG_STRATEGY_KERNEL_DIRECT;
+    if (is_smooth(n, 7)) return FYG_STRATEGY_MIX_RADIX;
+    if (is_prime(n) && n <= 78125 && 2 * n - 3 <= 78125) return FYG_STRATEGY_RADER;
+    if (n <= 39062) return FYG_STRATEGY_BLUESTEIN;
+    return FYG_STRATEGY_DFT;
+}
+
+// ------------------------------------------------------------------------------------------
+// Capacities and schedules
+// ------------------------------------------------------------------------------------------
+
+constexpr size_t kSmemLimit = 232448;  // 227 KB dynamic shared memory per CTA on sm_100/103
+constexpr int kMultiC = 8;             // columns per tile in multi-pass: 8 x 8 B = 64 B segments (fp32)
+
+template <typename T> static size_t colinfo_sz() { return sizeof(ColInfo<T>); }
+
+static size_t smem_for(int cb, int R, int C, int nst, int mid) {
+    return cb == 8 ? pass_smem_bytes<float>(R, C, nst, mid) : pass_smem_bytes<double>(R, C, nst, mid);
+}
+
+// radix schedule of an in-CTA transform of length R (13-smooth); empty if not representable
+static std::vector<int> radices_for(int R) {
+    std::vector<int> r;
+    int n = R, a = 0, b = 0;
+    while (n % 2 == 0) { n /= 2; ++a; }
+    while (n % 3 == 0) { n /= 3; ++b; }
+    std::vector<int> odd;
+    for (int p : {5, 7, 11, 13})
+        while (n % p == 0) { n /= p; odd.push_back(p); }
+    if (n != 1) return {};
+    while (a >= 4) { r.push_back(16); a -= 4; }
+    if (a == 3) r.push_back(8);
+    if (a == 2) r.push_back(4);
+    if (a == 1) r.push_back(2);
+    while (b >= 2) { r.push_back(9); b -= 2; }
+    if (b == 1) r.push_back(3);
+    for (int p : odd) r.push_back(p);
+    if (r.size() > (size_t)kMaxStages) return {};
+    return r;
+}
+
+static int max_single_R(int cb) {
+    // two ping-pong buffers of R complex plus one ColInfo
+    return (int)((kSmemLimit - 64) / (2 * (size_t)cb));
+}
+
+static int max_multi_R(int cb) {
+    return (int)((kSmemLimit - kMultiC * 64) / (2 * (size_t)cb * kMultiC));
+}
+
+// Split L into P >= 2 pass radices, each <= Rmax and representable; fewest passes, then fewest
+// in-CTA stages, then the most balanced split.
+static bool split_passes(uint64_t L, int Rmax, std::vector<int>& out) {
+    std::vector<int> divs;
+    for (int d = 4; d <= Rmax && (uint64_t)d <= L; ++d)
+        if (L % d == 0 && !radices_for(d).empty()) divs.push_back(d);
+    for (int P = 2; P <= 6; ++P) {
+        double best = 1e30;
+        std::vector<int> best_f, cur;
+        const double target = std::log((double)L) / P;
+        std::function<void(uint64_t, int)> rec = [&](uint64_t rem, int left) {
+            if (left == 1) {
+                if (rem > (uint64_t)Rmax || rem < 2) return;
+                std::vector<int> rr = radices_for((int)rem);
+                if (rr.empty()) return;
+                cur.push_back((int)rem);
+                double cost = 0;
+                for (int f : cur) cost += (double)radices_for(f).size() + 0.25 * std::fabs(std::log((double)f) - target);
+                if (cost < best) { best = cost; best_f = cur; }
+                cur.pop_back();
+                return;
+            }
+            for (int d : divs) {
+                if (rem % d) continue;
+                // remaining must fit in left-1 passes
+                double cap = std::pow((double)Rmax, left - 1);
+                if ((double)(rem / d) > cap) continue;
+                cur.push_back(d);
+                rec(rem / d, left - 1);
+                cur.pop_back();
+            }
+        };
+        rec(L, P);
+        if (!best_f.empty()) {
+            // larger radices first: the first pass writes fully contiguous R-runs
+            out = best_f;
+            return true;
+        }
+    }
+    return false;
+}
+
+static void fill_geom(TileGeom& g, int R, int C, bool colmajor, const std::vector<int>& rad) {
+    std::memset(&g, 0, sizeof(g));
+    g.R = R;
+    g.C = C;
+    int lc = 0;
+    while ((1 << lc) < C) ++lc;
+    g.log2C = lc;
+    g.colmajor = colmajor ? 1 : 0;
+    g.nst = (int)rad.size();
+    int ns = 1;
+    for (size_t s = 0; s < rad.size(); ++s) {
+        g.radix[s] = rad[s];
+        g.ns[s] = make_fastdiv((uint32_t)ns);
+        g.twmul[s] = R / (ns * rad[s]);
+        g.rr[s] = make_fastdiv((uint32_t)(R / rad[s]));
+        ns *= rad[s];
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Tables
+// ------------------------------------------------------------------------------------------
+
+static const long double kTwoPiL = 6.283185307179586476925286766559005768L;
+
+// exp(-2 pi i t/n) in long double with exact integer reduction of t
+static void twiddle_ld(uint64_t t, uint64_t n, long double* c, long double* s) {
+    t %= n;
+    // reduce to the first octant-friendly form: angle = 2 pi t / n, t < n
+    const long double a = kTwoPiL * (long double)t / (long double)n;
+    *c = cosl(a);
+    *s = -sinl(a);
+}
+
+static int upload_local_table(fyg_plan* pl, int R, int cb, const void** dptr) {
+    auto buf = std::make_unique<DevBuf>();
+    int rc;
+    if (cb == 8) {
+        std::vector<float2> h(R);
+        for (int t = 0; t < R; ++t) {
+            long double c, s;
+            twiddle_ld(t, R, &c, &s);
+            h[t] = make_float2((float)c, (float)s);
+        }
+        rc = buf->upload(h.data(), h.size() * sizeof(float2));
+    } else {
+        std::vector<double2> h(R);
+        for (int t = 0; t < R; ++t) {
+            long double c, s;
+            twiddle_ld(t, R, &c, &s);
+            h[t] = make_double2((double)c, (double)s);
+        }
+        rc = buf->upload(h.data(), h.size() * sizeof(double2));
+    }
+    if (rc) return rc;
+    *dptr = buf->ptr;
+    pl->tables.push_back(std::move(buf));
+    return FYG_OK;
+}
+
+// two-level table of w_L: hi[i] = w^(i 2^s), lo[j] = w^j; float tables hold (hi, lo) pairs
+static int upload_two_level(fyg_plan* pl, uint64_t L, int cb, const void** hi, const void** lo, int* shift) {
+    int s = 0;
+    while ((1ull << (2 * s)) < L) ++s;  // 2^s ~ sqrt(L)
+    if (s < 1) s = 1;
+    const uint64_t B = 1ull << s, nhi = (L + B - 1) / B;
+    auto bh = std::make_unique<DevBuf>(), bl = std::make_unique<DevBuf>();
+    int rc;
+    if (cb == 8) {
+        auto pack = [](long double c, long double sn) {
+            const float ch = (float)c, sh = (float)sn;
+            return make_float4(ch, sh, (float)(c - (long double)ch), (float)(sn - (long double)sh));
+        };
+        std::vector<float4> th(nhi), tl(B);
+        for (uint64_t i = 0; i < nhi; ++i) { long double c, sn; twiddle_ld(i * B, L, &c, &sn); th[i] = pack(c, sn); }
+        for (uint64_t j = 0; j < B; ++j) { long double c, sn; twiddle_ld(j, L, &c, &sn); tl[j] = pack(c, sn); }
+        rc = bh->upload(th.data(), th.size() * sizeof(float4));
+        if (!rc) rc = bl->upload(tl.data(), tl.size() * sizeof(float4));
+    } else {
+        std::vector<double2> th(nhi), tl(B);
+        for (uint64_t i = 0; i < nhi; ++i) { long double c, sn; twiddle_ld(i * B, L, &c, &sn); th[i] = make_double2((double)c, (double)sn); }
+        for (uint64_t j = 0; j < B; ++j) { long double c, sn; twiddle_ld(j, L, &c, &sn); tl[j] = make_double2((double)c, (double)sn); }
+        rc = bh->upload(th.data(), th.size() * sizeof(double2));
+        if (!rc) rc = bl->upload(tl.data(), tl.size() * sizeof(double2));
+    }
+    if (rc) return rc;
+    *hi = bh->ptr;
+    *lo = bl->ptr;
+    *shift = s;
+    pl->tables.push_back(std::move(bh));
+    pl->tables.push_back(std::move(bl));
+    return FYG_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// Pipelines
+// ------------------------------------------------------------------------------------------
+
+struct ConvTables {
+    const void* chirp = nullptr;
+    const int* gather = nullptr;
+    const int* scatter = nullptr;
+    const void* spectrum = nullptr;
+};
+
+struct PipeSpec {
+    int kind;                 // GS_*
+    uint64_t L;               // algorithm length
+    std::vector<int> prad;    // pass radices (size 1 for single-pass)
+    int C;                    // columns per tile (single-pass: transforms per CTA)
+};
+
+static int pick_variant(int compute_cb, int tin_cb, int tout_cb, int threads) {
+    if (compute_cb == 8) return threads <= 256 ? KV_F32_T256 : KV_F32_T1024;
+    if (tin_cb == 16 && tout_cb == 16) return threads <= 256 ? KV_F64_T256 : KV_F64_T512;
+    if (tin_cb == 8 && tout_cb == 16) return KV_F64_IF32_T512;
+    if (tin_cb == 16 && tout_cb == 8) return KV_F64_OF32_T512;
+    return KV_F64_F32IO_T512;
+}
+
+static int threads_for(int R, int C, int maxt) {
+    int t = (R * C + 15) / 16;
+    t = (t + 31) / 32 * 32;
+    t = std::max(t, 64);
+    return std::min(t, maxt);
+}
+
+static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
+                          const std::map<int, const void*>& local_tabs, const void* tw_hi,
+                          const void* tw_lo, int tw_shift, const ConvTables& ct,
+                          std::vector<PassDesc>& out) {
+    out.clear();
+    const int P = (int)ps.prad.size();
+    const bool conv = ps.kind == GS_RADER || ps.kind == GS_BLUESTEIN;
+    const int K = conv ? 2 * P - 1 : P;
+    const int cb = pl->compute_bytes;
+    const int io_cb = pl->dtype == FYG_C32 ? 8 : 16;
+    const uint64_t n = pl->n, L = ps.L;
+    uint64_t ns_fwd = 1, ns_inv = 1;
+    for (int i = 0; i < K; ++i) {
+        PassDesc d;
+        std::memset(&d.p, 0, sizeof(d.p));
+        PassParams& p = d.p;
+        const bool first = i == 0, last = i == K - 1;
+        const bool mid = conv && i == P - 1;
+        int R;
+        uint64_t Ns;
+        if (i < P) { R = ps.prad[i]; Ns = ns_fwd; ns_fwd *= R; }
+        else { R = ps.prad[K - 1 - i]; Ns = ns_inv; ns_inv *= R; }
+        if (mid) ns_inv = R;  // the mid pass also performs the first inverse pass (radix R, Ns 1)
+        const bool single = (P == 1);
+        const int C = single ? ps.C : kMultiC;
+        const std::vector<int> rad = radices_for(R);
+        fill_geom(p.g, R, C, single, rad);
+        p.Rr = (int)(L / R);
+        p.Ns = (int)Ns;
+        p.Ns_out = mid ? 1 : (int)Ns;
+        p.Lr = (int)(L / (Ns * R));
+        p.div_Rr = make_fastdiv((uint32_t)p.Rr);
+        p.div_Ns = make_fastdiv((uint32_t)p.Ns);
+        p.div_Ns_out = make_fastdiv((uint32_t)p.Ns_out);
+        p.tw_local = local_tabs.at(R);
+        p.tw_hi = tw_hi;
+        p.tw_lo = tw_lo;
+        p.tw_shift = tw_shift;
+        p.scale = 1.0;
+        p.scale2 = 1.0;
+        p.nvalid = (int64_t)n;
+        p.mid = mid ? 1 : 0;
+        p.spectrum = ct.spectrum;
+        p.chirp = ct.chirp;
+        p.gather = ct.gather;
+        p.scatter = ct.scatter;
+        p.err = reinterpret_cast<int*>(pl->errword.ptr);
+        d.in_role = first ? ROLE_IN : ((i - 1) % 2 == 0 ? ROLE_S0 : ROLE_S1);
+        d.out_role = last ? ROLE_OUT : (i % 2 == 0 ? ROLE_S0 : ROLE_S1);
+        d.in_elem_bytes = d.in_role == ROLE_IN ? io_cb : cb;
+        d.out_elem_bytes = d.out_role == ROLE_OUT ? io_cb : cb;
+        p.idist = d.in_role == ROLE_IN ? (int64_t)n : (int64_t)L;
+        p.odist = d.out_role == ROLE_OUT ? (int64_t)n : (int64_t)L;
+        // load / store fusions
+        p.load_mode = LD_PLAIN;
+        p.store_mode = ST_PLAIN;
+        if (first) {
+            p.conj_in = inverse ? 1 : 0;
+            if (ps.kind == GS_BLUESTEIN) p.load_mode = LD_CHIRP;
+            if (ps.kind == GS_RADER) { p.load_mode = LD_GATHER; p.x0_from_in = 1; }
+        }
+        if (mid && ps.kind == GS_RADER) p.dc_capture = 1;
+        if (last) {
+            if (ps.kind == GS_BLUESTEIN) {
+                p.store_mode = ST_CHIRP;
+                p.conj_out = inverse ? 0 : 1;
+                p.scale = inverse ? 1.0 / ((double)L * (double)n) : 1.0 / (double)L;
+            } else if (ps.kind == GS_RADER) {
+                p.store_mode = ST_SCATTER;
+                p.conj_out = inverse ? 0 : 1;
+                p.scale = 1.0 / (double)L;
+                p.scale2 = inverse ? 1.0 / (double)n : 1.0;
+            } else {
+                p.conj_out = inverse ? 1 : 0;
+                p.scale = inverse ? 1.0 / (double)n : 1.0;
+            }
+        }
+        const int maxt = cb == 8 ? 1024 : 512;
+        d.threads = threads_for(R, C, maxt);
+        d.kv = pick_variant(cb, (int)d.in_elem_bytes, (int)d.out_elem_bytes, d.threads);
+        d.threads = std::min(d.threads, variant_info(d.kv).maxt);
+        d.smem = smem_for(cb, R, C, (int)rad.size(), p.mid);
+        if (d.smem > kSmemLimit)
+            return set_error(FYG_ERR_UNSUPPORTED, "tile of " + std::to_string(R) + "x" + std::to_string(C) +
+                                                      " exceeds shared memory");
+        out.push_back(d);
+    }
+    return FYG_OK;
+}
+
+// FP64 transform of a host vector on the GPU (used to precompute convolution spectra).
+static int gpu_fft_f64(size_t n, const std::vector<double2>& h, std::vector<double2>& H);
+
+static int make_plan(fyg_plan* pl) {
+    const uint64_t n = pl->n;
+    const int io_cb = pl->dtype == FYG_C32 ? 8 : 16;
+    PipeSpec ps;
+    ps.C = 1;
+    ConvTables ct;
+    std::vector<double2> kernel_time;   // convolution kernel (time domain), FP64
+    std::vector<int> gather, scatter;
+    std::vector<float2> chirp_f;
+    std::vector<double2> chirp_d;
+
+    if (n == 1) {
+        pl->strategy = GS_COPY;
+        pl->L = 1;
+        pl->compute_bytes = io_cb;
+        return FYG_OK;
+    }
+    // ---- strategy ----
+    const int single_cap_io = max_single_R(io_cb);
+    if (is_smooth(n, 13) && n <= (uint64_t)single_cap_io && !radices_for((int)n).empty()) {
+        ps.kind = GS_SINGLE;
+        ps.L = n;
+        ps.prad = {(int)n};
+    } else if (is_smooth(n, 13)) {
+        ps.kind = GS_MULTI;
+        ps.L = n;
+    } else if (is_prime(n) && (is_smooth(n - 1, 13) || 2 * n - 3 <= 78125)) {
+        ps.kind = GS_RADER;
+        const uint64_t Lc = n - 1;
+        ps.L = is_smooth(Lc, 13) ? Lc : next_smooth7(2 * Lc - 1);
+    } else {
+        ps.kind = GS_BLUESTEIN;
+        ps.L = next_smooth7(2 * n - 1);
+    }
+    pl->strategy = ps.kind;
+    pl->L = ps.L;
+    const bool conv = ps.kind == GS_RADER || ps.kind == GS_BLUESTEIN;
+    if (conv && pl->dtype == FYG_C32) {
+        if (pl->flags & FYG_FLAG_CONV_FP64) pl->conv_fp64 = 1;
+        else pl->conv_fp64 = 0;
+    }
+    pl->compute_bytes = (pl->dtype == FYG_C64 || pl->conv_fp64) ? 16 : 8;
+    const int cb = pl->compute_bytes;
+    if (ps.kind != GS_SINGLE) {
+        if (conv && ps.L <= (uint64_t)max_single_R(cb) && !radices_for((int)ps.L).empty()) {
+            ps.prad = {(int)ps.L};
+        } else if (!split_passes(ps.L, max_multi_R(cb), ps.prad)) {
+            return set_error(FYG_ERR_UNSUPPORTED, "no pass decomposition for length " + std::to_string(ps.L));
+        }
+    }
+    const int P = (int)ps.prad.size();
+    if (P == 1) {
+        // several transforms per CTA for small lengths
+        const int target = cb == 8 ? 4096 : 2048;
+        int C = std::max(1, target / (int)ps.L);
+        C = (int)std::min<uint64_t>((uint64_t)C, pl->batch);
+        C = std::min(C, 256);
+        ps.C = std::max(C, 1);
+    }
+    // ---- chunking: keep the scratch of one chunk L2-resident ----
+    const int K = conv ? 2 * P - 1 : P;
+    if (K == 1) pl->chunk = pl->batch;
+    else {
+        const uint64_t chunk_elems = (32ull << 20) / cb;  // 32 MB per scratch buffer
+        uint64_t c = std::max<uint64_t>(1, chunk_elems / ps.L);
+        if (pl->flags & FYG_FLAG_NO_L2_CHUNK) c = pl->batch;
+        pl->chunk = (size_t)std::min<uint64_t>(c, pl->batch);
+    }
+    // column indices are 32-bit inside the kernels
+    const uint64_t maxRr = ps.L / *std::min_element(ps.prad.begin(), ps.prad.end());
+    if ((uint64_t)pl->chunk * maxRr >= (1ull << 31) || ps.L >= (1ull << 31))
+        return set_error(FYG_ERR_INVALID_LENGTH, "length/batch too large for 32-bit tile indexing");
+
+    int rc = pl->errword.alloc(16);
+    if (rc) return rc;
+    cudaMemset(pl->errword.ptr, 0, 16);
+    // ---- tables ----
+    std::map<int, const void*> local_tabs;
+    for (int R : ps.prad)
+        if (!local_tabs.count(R)) {
+            const void* d = nullptr;
+            rc = upload_local_table(pl, R, cb, &d);
+            if (rc) return rc;
+            local_tabs[R] = d;
+        }
+    const void *tw_hi = nullptr, *tw_lo = nullptr;
+    int tw_shift = 1;
+    if (P > 1) {
+        rc = upload_two_level(pl, ps.L, cb, &tw_hi, &tw_lo, &tw_shift);
+        if (rc) return rc;
+    }
+    if (ps.kind == GS_BLUESTEIN) {
+        // chirp w[k] = exp(+i pi (k^2 mod 2N) / N), exact integer reduction, long double
+        const uint64_t twoN = 2 * n, M = ps.L;
+        std::vector<long double> wc(n), ws(n);
+        for (uint64_t k = 0; k < n; ++k) {
+            const uint64_t sq = mulmod(k, k, twoN);
+            const long double a = kTwoPiL * 0.5L * (long double)sq / (long double)n;
+            wc[k] = cosl(a);
+            ws[k] = sinl(a);
+        }
+        kernel_time.assign(M, make_double2(0, 0));
+        kernel_time[0] = make_double2((double)wc[0], (double)ws[0]);
+        for (uint64_t k = 1; k < n; ++k) {
+            kernel_time[k] = make_double2((double)wc[k], (double)ws[k]);
+            kernel_time[M - k] = kernel_time[k];
+        }
+        auto buf = std::make_unique<DevBuf>();
+        if (cb == 8) {
+            chirp_f.resize(n);
+            for (uint64_t k = 0; k < n; ++k) chirp_f[k] = make_float2((float)wc[k], (float)ws[k]);
+            rc = buf->upload(chirp_f.data(), n * sizeof(float2));
+        } else {
+            chirp_d.resize(n);
+            for (uint64_t k = 0; k < n; ++k) chirp_d[k] = make_double2((double)wc[k], (double)ws[k]);
+            rc = buf->upload(chirp_d.data(), n * sizeof(double2));
+        }
+        if (rc) return rc;
+        ct.chirp = buf->ptr;
+        pl->tables.push_back(std::move(buf));
+    } else if (ps.kind == GS_RADER) {
+        const uint64_t Lc = n - 1, M = ps.L, g = primitive_root(n), ginv = powmod(g, n - 2, n);
+        gather.assign(M, -1);
+        scatter.assign(M, -1);
+        std::vector<uint64_t> gp(Lc);
+        uint64_t cur = 1, curi = 1;
+        for (uint64_t i = 0; i < Lc; ++i) {
+            gp[i] = cur;
+            gather[i] = (int)curi;
+            cur = mulmod(cur, g, n);
+            curi = mulmod(curi, ginv, n);
+        }
+        kernel_time.assign(M, make_double2(0, 0));
+        if (M == Lc) {
+            for (uint64_t q = 0; q < Lc; ++q) scatter[q] = (int)gp[q];
+            for (uint64_t p = 0; p < Lc; ++p) {
+                long double c, s;
+                twiddle_ld(gp[p], n, &c, &s);
+                kernel_time[p] = make_double2((double)c, (double)s);
+            }
+        } else {
+            // zero-padded linear convolution; outputs q in [L-1, 2L-1) carry the cyclic result
+            for (uint64_t q = Lc - 1; q < 2 * Lc - 1; ++q) scatter[q] = (int)gp[q % Lc];
+            for (uint64_t m = 0; m < M; ++m) {
+                long double c, s;
+                twiddle_ld(gp[m % Lc], n, &c, &s);
+                kernel_time[m] = make_double2((double)c, (double)s);
+            }
+        }
+        auto bg = std::make_unique<DevBuf>(), bs = std::make_unique<DevBuf>();
+        rc = bg->upload(gather.data(), M * sizeof(int));
+        if (!rc) rc = bs->upload(scatter.data(), M * sizeof(int));
+        if (rc) return rc;
+        ct.gather = reinterpret_cast<const int*>(bg->ptr);
+        ct.scatter = reinterpret_cast<const int*>(bs->ptr);
+        pl->tables.push_back(std::move(bg));
+        pl->tables.push_back(std::move(bs));
+        rc = pl->x0buf.alloc(pl->chunk * cb);
+        if (!rc) rc = pl->dcbuf.alloc(pl->chunk * cb);
+        if (rc) return rc;
+    }
+    if (conv) {
+        // spectrum of the convolution kernel: FP64 GPU FFT of the long-double kernel, rounded once
+        std::vector<double2> H;
+        rc = gpu_fft_f64(ps.L, kernel_time, H);
+        if (rc) return rc;
+        auto buf = std::make_unique<DevBuf>();
+        if (cb == 8) {
+            std::vector<float2> Hf(ps.L);
+            for (uint64_t i = 0; i < ps.L; ++i) Hf[i] = make_float2((float)H[i].x, (float)H[i].y);
+            rc = buf->upload(Hf.data(), ps.L * sizeof(float2));
+        } else {
+            rc = buf->upload(H.data(), ps.L * sizeof(double2));
+        }
+        if (rc) return rc;
+        ct.spectrum = buf->ptr;
+        pl->tables.push_back(std::move(buf));
+    }
+    // ---- scratch ----
+    if (K >= 2) {
+        rc = pl->scratch0.alloc(pl->chunk * ps.L * cb);
+        if (!rc && K >= 3) rc = pl->scratch1.alloc(pl->chunk * ps.L * cb);
+        if (rc) return rc;
+    }
+    rc = build_pipeline(pl, ps, false, local_tabs, tw_hi, tw_lo, tw_shift, ct, pl->fwd);
+    if (!rc) rc = build_pipeline(pl, ps, true, local_tabs, tw_hi, tw_lo, tw_shift, ct, pl->inv);
+    return rc;
+}
+
+// ------------------------------------------------------------------------------------------
+// Execution
+// ------------------------------------------------------------------------------------------
+
+static int run_pipeline(fyg_plan* pl, const std::vector<PassDesc>& pipe, const void* in, void* out,
+                        double final_scale_mul, cudaStream_t st) {
+    const int io_cb = pl->dtype == FYG_C32 ? 8 : 16;
+    for (size_t c0 = 0; c0 < pl->batch; c0 += pl->chunk) {
+        const size_t nb = std::min(pl->chunk, pl->batch - c0);
+        for (size_t i = 0; i < pipe.size(); ++i) {
+            const PassDesc& d = pipe[i];
+            PassParams p = d.p;
+            auto resolve = [&](int role) -> void* {
+                switch (role) {
+                    case ROLE_IN: return (void*)((const char*)in + c0 * pl->n * io_cb);
+                    case ROLE_OUT: return (void*)((char*)out + c0 * pl->n * io_cb);
+                    case ROLE_S0: return pl->scratch0.ptr;
+                    default: return pl->scratch1.ptr;
+                }
+            };
+            p.in = resolve(d.in_role);
+            p.out = resolve(d.out_role);
+            p.ncols = (int64_t)nb * p.Rr;
+            p.x0buf = pl->x0buf.ptr;
+            p.dcbuf = pl->dcbuf.ptr;
+            if (i + 1 == pipe.size()) {
+                if (p.store_mode == ST_SCATTER) p.scale2 *= final_scale_mul;
+                else p.scale *= final_scale_mul;
+            }
+            const unsigned grid = (unsigned)((p.ncols + p.g.C - 1) / p.g.C);
+            cudaError_t e = launch_pass(d.kv, p, grid, d.threads, d.smem, st);
+            if (e != cudaSuccess) return cuda_error(e, "tile pass launch");
+        }
+    }
+    return FYG_OK;
+}
+
+static bool is_device_ptr(const void* ptr) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+static int execute_dir(fyg_plan* pl, const void* in, void* out, bool inverse, double scale_mul, cudaStream_t st) {
+    if (!pl) return set_error(FYG_ERR_NULL_PTR, "null plan");
+    if (!in || !out) return set_error(FYG_ERR_NULL_PTR, "null buffer");
+    const int io_cb = pl->dtype == FYG_C32 ? 8 : 16;
+    if (((uintptr_t)in % io_cb) || ((uintptr_t)out % io_cb))
+        return set_error(FYG_ERR_MISALIGNED, "buffers must be aligned to the complex element size");
+    int cur = 0;
+    cudaGetDevice(&cur);
+    if (cur != pl->device) cudaSetDevice(pl->device);
+    const size_t bytes = pl->n * pl->batch * io_cb;
+    const bool din = is_device_ptr(in), dout = is_device_ptr(out);
+    const void* din_p = in;
+    void* dout_p = out;
+    int rc = FYG_OK;
+    if (!din || !dout) {
+        if (pl->stage_in_bytes < bytes) {
+            rc = pl->stage_in.alloc(bytes);
+            if (!rc) rc = pl->stage_out.alloc(bytes);
+            if (rc) return rc;
+            pl->stage_in_bytes = bytes;
+        }
+        if (!din) {
+            cudaError_t e = cudaMemcpyAsync(pl->stage_in.ptr, in, bytes, cudaMemcpyHostToDevice, st);
+            if (e != cudaSuccess) return cuda_error(e, "host->device staging");
+            din_p = pl->stage_in.ptr;
+        }
+        if (!dout) dout_p = pl->stage_out.ptr;
+    }
+    if (pl->strategy == GS_COPY) {
+        cudaError_t e = launch_scale_copy(din_p, dout_p, pl->batch, pl->dtype, scale_mul, 0, st);
+        if (e != cudaSuccess) return cuda_error(e, "copy");
+    } else {
+        rc = run_pipeline(pl, inverse ? pl->inv : pl->fwd, din_p, dout_p, scale_mul, st);
+        if (rc) return rc;
+    }
+    if (!dout) {
+        cudaError_t e = cudaMemcpyAsync(out, dout_p, bytes, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) return cuda_error(e, "device->host staging");
+    }
+    if (!din || !dout) {
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return cuda_error(e, "stream synchronize");
+    }
+    if (cur != pl->device) cudaSetDevice(cur);
+    return FYG_OK;
+}
+
+static int gpu_fft_f64(size_t n, const std::vector<double2>& h, std::vector<double2>& H) {
+    fyg_plan* sub = nullptr;
+    int rc = fyg_plan_create(n, FYG_C64, 1, 0, &sub);
+    if (rc) return rc;
+    DevBuf a, b;
+    rc = a.upload(h.data(), n * sizeof(double2));
+    if (!rc) rc = b.alloc(n * sizeof(double2));
+    if (!rc) rc = execute_dir(sub, a.ptr, b.ptr, false, 1.0, 0);
+    if (!rc) {
+        H.resize(n);
+        cudaError_t e = cudaMemcpy(H.data(), b.ptr, n * sizeof(double2), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) rc = cuda_error(e, "spectrum download");
+    }
+    fyg_plan_destroy(sub);
+    return rc;
+}
+
+}  // namespace fyg
+
+// ------------------------------------------------------------------------------------------
+// C ABI (plans)
+// ------------------------------------------------------------------------------------------
+
+using namespace fyg;
+
+extern "C" {
+
+int fyg_plan_create(size_t n, int dtype, size_t batch, int flags, fyg_plan** out) {
+    clear_error();
+    if (!out) return set_error(FYG_ERR_NULL_PTR, "out is null");
+    *out = nullptr;
+    if (n < 1) return set_error(FYG_ERR_INVALID_LENGTH, "length must be >= 1");
+    if (batch < 1) return set_error(FYG_ERR_INVALID_ARG, "batch must be >= 1");
+    if (dtype != FYG_C32 && dtype != FYG_C64) return set_error(FYG_ERR_INVALID_ARG, "dtype must be FYG_C32 or FYG_C64");
+    if (n >= (1ull << 31)) return set_error(FYG_ERR_INVALID_LENGTH, "length must be < 2^31");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+    e = ensure_device_constants();
+    if (e != cudaSuccess) return cuda_error(e, "codelet constants");
+    auto* pl = new fyg_plan();
+    pl->n = n;
+    pl->batch = batch;
+    pl->dtype = dtype;
+    pl->flags = flags;
+    pl->device = dev;
+    int rc = make_plan(pl);
+    if (rc) {
+        delete pl;
+        return rc;
+    }
+    *out = pl;
+    return FYG_OK;
+}
+
+int fyg_plan_destroy(fyg_plan* plan) {
+    delete plan;
+    return FYG_OK;
+}
+
+int fyg_execute(fyg_plan* plan, const void* in, void* out, int direction, void* stream) {
+    clear_error();
+    if (direction != FYG_FORWARD && direction != FYG_INVERSE)
+        return set_error(FYG_ERR_INVALID_ARG, "direction must be FYG_FORWARD or FYG_INVERSE");
+    return execute_dir(plan, in, out, direction == FYG_INVERSE, 1.0, (cudaStream_t)stream);
+}
+
+int fyg_execute_adjoint(fyg_plan* plan, const void* g, void* out, double scale, void* stream) {
+    clear_error();
+    if (!plan) return set_error(FYG_ERR_NULL_PTR, "null plan");
+    // F^H g = N * IFFT(g): the inverse pipeline with its 1/N replaced by `scale`
+    return execute_dir(plan, g, out, true, scale * (double)plan->n, (cudaStream_t)stream);
+}
+
+int fyg_strategy(size_t n) { return ref_strategy(n); }
+
+int fyg_gpu_strategy(size_t n) {
+    if (n < 2) return -1;
+    if (is_smooth(n, 7)) return ref_directly_supported(n) ? FYG_STRATEGY_KERNEL_DIRECT : FYG_STRATEGY_MIX_RADIX;
+    if (is_smooth(n, 13)) return FYG_STRATEGY_MIX_RADIX;
+    if (is_prime(n) && (is_smooth(n - 1, 13) || 2 * n - 3 <= 78125)) return FYG_STRATEGY_RADER;
+    return FYG_STRATEGY_BLUESTEIN;
+}
+
+int fyg_plan_info(const fyg_plan* plan, size_t* conv_length, int* passes, int* strategy) {
+    if (!plan) return set_error(FYG_ERR_NULL_PTR, "null plan");
+    if (conv_length) *conv_length = plan->L;
+    if (passes) *passes = (int)plan->fwd.size();
+    if (strategy) *strategy = plan->strategy;
+    return FYG_OK;
+}
+
+const char* fyg_last_error_string(void) { return last_error(); }
+
+int fyg_fill_random(uint64_t seed, int dist, int dtype, size_t n_complex, void* out) {
+    if (!out && n_complex) return set_error(FYG_ERR_NULL_PTR, "null buffer");
+    if (dtype != FYG_C32 && dtype != FYG_C64) return set_error(FYG_ERR_INVALID_ARG, "bad dtype");
+    fill_random_host(seed, dist, dtype, n_complex, out);
+    return FYG_OK;
+}
+
+int fyg_fill_random_device(uint64_t seed, int dist, int dtype, size_t n_complex, void* out, void* stream) {
+    if (!out && n_complex) return set_error(FYG_ERR_NULL_PTR, "null buffer");
+    if (dtype != FYG_C32 && dtype != FYG_C64) return set_error(FYG_ERR_INVALID_ARG, "bad dtype");
+    cudaError_t e = launch_fill_random(seed, dist, dtype, n_complex, out, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_error(e, "fill_random_device");
+    return FYG_OK;
+}
+
+const char* fyg_version(void) { return "fyfft-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

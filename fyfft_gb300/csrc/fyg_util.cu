@@ -1,0 +1,177 @@
+// fyg_util.cu -- per-device constants, seeded synthetic data, small helper kernels.
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "fyg_internal.h"
+#include "fyg_host.h"
+
+namespace fyg {
+
+cudaError_t upload_consts_f32(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd);
+cudaError_t upload_consts_f64(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd);
+cudaError_t upload_consts_mixed(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd);
+
+namespace {
+
+template <typename T>
+void fill_consts(CodeletConsts<T>& K) {
+    const long double two_pi = 6.283185307179586476925286766559005768L;
+    auto put = [&](T* c, T* s, int r) {
+        for (int m = 0; m < r; ++m) {
+            const long double a = two_pi * (long double)m / (long double)r;
+            c[m] = (T)cosl(a);
+            s[m] = (T)sinl(a);
+        }
+    };
+    put(K.c3, K.s3, 3);
+    put(K.c5, K.s5, 5);
+    put(K.c7, K.s7, 7);
+    put(K.c9, K.s9, 9);
+    put(K.c11, K.s11, 11);
+    put(K.c13, K.s13, 13);
+    put(K.c16, K.s16, 16);
+}
+
+std::mutex g_init_mu;
+bool g_dev_init[128] = {};
+
+}  // namespace
+
+cudaError_t ensure_device_constants() {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    if (dev < 128 && g_dev_init[dev]) return cudaSuccess;
+    CodeletConsts<float> kf;
+    CodeletConsts<double> kd;
+    fill_consts(kf);
+    fill_consts(kd);
+    e = upload_consts_f32(kf, kd);
+    if (e == cudaSuccess) e = upload_consts_f64(kf, kd);
+    if (e == cudaSuccess) e = upload_consts_mixed(kf, kd);
+    if (e == cudaSuccess && dev < 128) g_dev_init[dev] = true;
+    return e;
+}
+
+// ------------------------------------------------------------------------------------------
+// Seeded synthetic data: element i of stream `seed` is a pure function of (seed, i), so host
+// and device generate the same values and generation parallelizes.
+// ------------------------------------------------------------------------------------------
+
+__host__ __device__ inline uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__host__ __device__ inline uint64_t rand_bits(uint64_t seed, uint64_t i) {
+    return mix64(mix64(seed + 0x9E3779B97F4A7C15ull) + (i + 1) * 0x9E3779B97F4A7C15ull);
+}
+
+// uniform: re, im in [-1, 1); normal: Box-Muller on two 53-bit uniforms
+__host__ __device__ inline void rand_pair(uint64_t seed, uint64_t i, int dist, double* re, double* im) {
+    const uint64_t b1 = rand_bits(seed, 2 * i), b2 = rand_bits(seed, 2 * i + 1);
+    const double u1 = (double)(b1 >> 11) * 0x1.0p-53;
+    const double u2 = (double)(b2 >> 11) * 0x1.0p-53;
+    if (dist == 0) {
+        *re = 2.0 * u1 - 1.0;
+        *im = 2.0 * u2 - 1.0;
+    } else {
+        const double r = sqrt(-2.0 * log(1.0 - u1));  // 1 - u1 in (0, 1]
+        *re = r * cos(6.283185307179586 * u2);
+        *im = r * sin(6.283185307179586 * u2);
+    }
+}
+
+__global__ void k_fill_random(uint64_t seed, int dist, int dtype, size_t n, void* out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        double re, im;
+        rand_pair(seed, i, dist, &re, &im);
+        if (dtype == 0) reinterpret_cast<float2*>(out)[i] = make_float2((float)re, (float)im);
+        else reinterpret_cast<double2*>(out)[i] = make_double2(re, im);
+    }
+}
+
+cudaError_t launch_fill_random(uint64_t seed, int dist, int dtype, size_t n, void* out, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    k_fill_random<<<blocks, 256, 0, st>>>(seed, dist, dtype, n, out);
+    return cudaGetLastError();
+}
+
+void fill_random_host(uint64_t seed, int dist, int dtype, size_t n, void* out) {
+    auto work = [=](size_t lo, size_t hi) {
+        for (size_t i = lo; i < hi; ++i) {
+            double re, im;
+            rand_pair(seed, i, dist, &re, &im);
+            if (dtype == 0) {
+                reinterpret_cast<float*>(out)[2 * i] = (float)re;
+                reinterpret_cast<float*>(out)[2 * i + 1] = (float)im;
+            } else {
+                reinterpret_cast<double*>(out)[2 * i] = re;
+                reinterpret_cast<double*>(out)[2 * i + 1] = im;
+            }
+        }
+    };
+    unsigned nt = std::thread::hardware_concurrency();
+    if (nt == 0) nt = 1;
+    if (n < (1u << 16) || nt == 1) { work(0, n); return; }
+    nt = std::min(nt, 32u);
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; ++t) th.emplace_back(work, n * t / nt, n * (t + 1) / nt);
+    for (auto& x : th) x.join();
+}
+
+__global__ void k_convert_d2f(const double2* in, float2* out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = make_float2((float)in[i].x, (float)in[i].y);
+}
+
+cudaError_t launch_convert_d2f(const double2* in, float2* out, size_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    k_convert_d2f<<<blocks, 256, 0, st>>>(in, out, n);
+    return cudaGetLastError();
+}
+
+template <typename T2>
+__global__ void k_scale_copy(const T2* in, T2* out, size_t n, double scale, int conj) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        T2 v = in[i];
+        v.x = (decltype(v.x))(v.x * scale);
+        v.y = (decltype(v.y))((conj ? -v.y : v.y) * scale);
+        out[i] = v;
+    }
+}
+
+// out = scale * in (length-1 transforms are the identity)
+cudaError_t launch_scale_copy(const void* in, void* out, size_t n, int dtype, double scale, int conj,
+                              cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    if (dtype == 0) k_scale_copy<float2><<<blocks, 256, 0, st>>>((const float2*)in, (float2*)out, n, scale, conj);
+    else k_scale_copy<double2><<<blocks, 256, 0, st>>>((const double2*)in, (double2*)out, n, scale, conj);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------------
+// Errors
+// ------------------------------------------------------------------------------------------
+
+static thread_local std::string t_last_error;
+
+int set_error(int code, const std::string& msg) {
+    t_last_error = msg;
+    return code;
+}
+void clear_error() { t_last_error.clear(); }
+const char* last_error() { return t_last_error.c_str(); }
+
+int cuda_error(cudaError_t e, const char* what) {
+    return set_error(FYG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+}  // namespace fyg

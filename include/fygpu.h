@@ -1,0 +1,126 @@
+/*
+ * fygpu.h -- C ABI of the GB300 (sm_103a) 1D complex FFT library (libfygpu.so).
+ *
+ * Drop-in GPU path for fyFFT's plan/execute API (kjear/fyFFT, foye_FFT.hpp).  Every function
+ * returns an int status (FYG_OK == 0); fyg_last_error_string() describes the last failure on
+ * the calling thread.  Plain pointers and sizes only: streams are passed as void* holding a
+ * cudaStream_t (NULL = the legacy default stream).
+ *
+ * Data layout: interleaved complex, `dtype` FYG_C32 (re,im float pairs, the reference's
+ * `float*` buffers) or FYG_C64 (double pairs).  Forward is exp(-2 pi i kn/N); inverse is
+ * exp(+2 pi i kn/N) scaled by 1/N, as in the reference (e.g. src/foye_FFT_radix2.hpp:669-672).
+ *
+ * Threading: a plan is not thread-safe (it owns mutable scratch, like the reference's
+ * mixed-radix, Rader and Bluestein plans); use one plan per host thread or serialize calls.
+ */
+#ifndef FYGPU_H_
+#define FYGPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FYG_OK 0
+#define FYG_ERR_INVALID_LENGTH 1
+#define FYG_ERR_NULL_PTR 2
+#define FYG_ERR_MISALIGNED 3
+#define FYG_ERR_ALLOC 4
+#define FYG_ERR_CUDA 5
+#define FYG_ERR_TIMEOUT 6
+#define FYG_ERR_INVALID_ARG 7
+#define FYG_ERR_UNSUPPORTED 8
+
+/* element types */
+#define FYG_C32 0
+#define FYG_C64 1
+
+/* directions */
+#define FYG_FORWARD 1
+#define FYG_INVERSE (-1)
+
+/* execution strategies, numbered like fy::fft::FFT1D_C2C_invoker::FFT_execution_strategy
+ * (foye_FFT.hpp:153-160) */
+#define FYG_STRATEGY_KERNEL_DIRECT 0
+#define FYG_STRATEGY_MIX_RADIX 1
+#define FYG_STRATEGY_RADER 2
+#define FYG_STRATEGY_BLUESTEIN 3
+#define FYG_STRATEGY_DFT 4
+
+/* plan flags */
+#define FYG_FLAG_CONV_FP64 0x1   /* Rader/Bluestein convolution in FP64 even for FYG_C32 data */
+#define FYG_FLAG_CONV_FP32 0x2   /* force the FP32 convolution (disables the error-budget choice) */
+#define FYG_FLAG_NO_L2_CHUNK 0x4 /* process the whole batch per pass (no L2-resident chunking) */
+
+typedef struct fyg_plan fyg_plan;
+typedef struct fyg_batch fyg_batch;
+
+/* Creates a plan for `batch` contiguous transforms of length n (n >= 1).
+ * Replaces fy::fft::FFT1D_C2C_invoker::FFT1D_C2C_invoker(std::size_t) (foye_FFT.hpp:101-126):
+ * the constructor's strategy choice and table/workspace set-up happen here, once. */
+int fyg_plan_create(size_t n, int dtype, size_t batch, int flags, fyg_plan** out);
+
+/* Releases the plan and its device tables and scratch. */
+int fyg_plan_destroy(fyg_plan* plan);
+
+/* Runs the batch: direction FYG_FORWARD or FYG_INVERSE (1/N).  `in` and `out` are device
+ * pointers, or host pointers (staged through device buffers and synchronized before return).
+ * in == out (in place) is allowed.
+ * Replaces fy::fft::FFT1D_C2C_invoker::dispatch<bool invert>(const float*, float*)
+ * (foye_FFT.hpp:128-151); the reference runs one transform per call. */
+int fyg_execute(fyg_plan* plan, const void* in, void* out, int direction, void* stream);
+
+/* Adjoint (conjugate transpose) of the forward transform, times `scale`:
+ * out = scale * F^H g = scale * N * dispatch<true>(g).  No counterpart in the reference; its
+ * backward transform scaled by N is the reference gradient it is checked against. */
+int fyg_execute_adjoint(fyg_plan* plan, const void* g, void* out, double scale, void* stream);
+
+/* Strategy the reference would choose for n: fy::fft::FFT1D_C2C_invoker::
+ * acquired_execution_strategy(std::size_t) (foye_FFT.hpp:162-184).  Returns -1 for n < 2. */
+int fyg_strategy(size_t n);
+
+/* Strategy this library runs for n (never FYG_STRATEGY_DFT). */
+int fyg_gpu_strategy(size_t n);
+
+/* Plan introspection: algorithm length (conv length M for Rader/Bluestein), number of kernel
+ * passes per direction, and the GPU strategy. */
+int fyg_plan_info(const fyg_plan* plan, size_t* conv_length, int* passes, int* strategy);
+
+/* Uneven batch: `count` transforms with the given lengths, packed back to back (element
+ * offsets given at execute time).  One persistent kernel runs them all from a device work
+ * queue.  No counterpart in the reference (it runs one transform per call). */
+int fyg_batch_create(const size_t* lengths, size_t count, int dtype, int flags, fyg_batch** out);
+int fyg_batch_destroy(fyg_batch* batch);
+
+/* offsets_dev: device array of `count` int64 element offsets (NULL: packed back to back in the
+ * order given).  in/out device pointers. */
+int fyg_batch_execute(fyg_batch* batch, const void* in, void* out, const int64_t* offsets_dev,
+                      int direction, void* stream);
+
+/* Same batch, one launch sequence per transform (the plain one-plan-per-launch path). */
+int fyg_batch_execute_plain(fyg_batch* batch, const void* in, void* out, int direction,
+                            void* stream);
+
+/* Last error on the calling thread ("" if none). */
+const char* fyg_last_error_string(void);
+
+/* Seeded synthetic data (host, no GPU): counter-based splitmix64 stream; dist 0 = uniform
+ * [-1, 1), 1 = standard normal (Box-Muller).  n_complex complex elements of `dtype` written
+ * to `out` (re then im per element); element i depends only on (seed, i). */
+int fyg_fill_random(uint64_t seed, int dist, int dtype, size_t n_complex, void* out);
+
+/* Same stream generated on the device into device memory. */
+int fyg_fill_random_device(uint64_t seed, int dist, int dtype, size_t n_complex, void* out,
+                           void* stream);
+
+/* Library version string. */
+const char* fyg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FYGPU_H_ */
