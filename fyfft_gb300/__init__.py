@@ -33,7 +33,8 @@ FYG_FLAG_CONV_FP64, FYG_FLAG_CONV_FP32, FYG_FLAG_NO_L2_CHUNK = 1, 2, 4
 # every symbol include/fygpu.h declares
 EXPORTED_SYMBOLS = (
     "fyg_plan_create", "fyg_plan_destroy", "fyg_execute", "fyg_execute_adjoint", "fyg_strategy",
-    "fyg_gpu_strategy", "fyg_plan_info", "fyg_batch_create", "fyg_batch_destroy",
+    "fyg_gpu_strategy", "fyg_plan_info", "fyg_plan_launches", "fyg_plan_profile",
+    "fyg_plan_profile_read", "fyg_batch_create", "fyg_batch_destroy",
     "fyg_batch_execute", "fyg_batch_execute_plain", "fyg_last_error_string", "fyg_fill_random",
     "fyg_fill_random_device", "fyg_version",
 )
@@ -72,6 +73,10 @@ def lib() -> ctypes.CDLL:
         L.fyg_strategy.argtypes = [sz]
         L.fyg_gpu_strategy.argtypes = [sz]
         L.fyg_plan_info.argtypes = [vp, ctypes.POINTER(sz), ctypes.POINTER(i), ctypes.POINTER(i)]
+        L.fyg_plan_launches.argtypes = [vp, ctypes.POINTER(i)]
+        L.fyg_plan_profile.argtypes = [vp, i]
+        L.fyg_plan_profile_read.argtypes = [vp, ctypes.POINTER(d), ctypes.POINTER(ctypes.c_int64),
+                                            ctypes.POINTER(ctypes.c_int64), i, ctypes.POINTER(i)]
         L.fyg_batch_create.argtypes = [ctypes.POINTER(sz), sz, i, i, ctypes.POINTER(vp)]
         L.fyg_batch_destroy.argtypes = [vp]
         L.fyg_batch_execute.argtypes = [vp, vp, vp, vp, i, vp]
@@ -198,6 +203,24 @@ class FFT1D_C2C_invoker:
         L, P, S = ctypes.c_size_t(), ctypes.c_int(), ctypes.c_int()
         check(lib().fyg_plan_info(self._h, ctypes.byref(L), ctypes.byref(P), ctypes.byref(S)))
         return {"conv_length": L.value, "passes": P.value, "gpu_strategy": S.value}
+
+    def launches(self) -> int:
+        n = ctypes.c_int()
+        check(lib().fyg_plan_launches(self._h, ctypes.byref(n)))
+        return n.value
+
+    def profile(self, enable: bool = True) -> None:
+        check(lib().fyg_plan_profile(self._h, int(enable)))
+
+    def profile_read(self):
+        """[(total_ms, launches, bytes_per_launch)] per forward pass (synchronizes)."""
+        m = 32
+        ms = (ctypes.c_double * m)()
+        ln = (ctypes.c_int64 * m)()
+        by = (ctypes.c_int64 * m)()
+        n = ctypes.c_int()
+        check(lib().fyg_plan_profile_read(self._h, ms, ln, by, m, ctypes.byref(n)))
+        return [(ms[i], ln[i], by[i]) for i in range(min(n.value, m))]
 
     @staticmethod
     def acquired_execution_strategy(length: int) -> FFT_execution_strategy:

@@ -45,15 +45,14 @@ struct FastDiv {
     __device__ __forceinline__ uint32_t div(uint32_t n) const { return (__umulhi(n, m) + n) >> s; }
 };
 
-// Codelet constants: C[m] = cos(2 pi m/r), S[m] = sin(2 pi m/r).
+// Codelet constants: C[m] = cos(2 pi m/r), S[m] = sin(2 pi m/r) for every codelet size r that
+// needs them (odd primes, and the composite sizes for their internal twiddles).
+#define FYG_CODELET_TABLES(X) \
+    X(3) X(5) X(7) X(9) X(11) X(13) X(16) X(12) X(20) X(24) X(25) X(27) X(32)
 template <typename T> struct CodeletConsts {
-    T c3[3], s3[3];
-    T c5[5], s5[5];
-    T c7[7], s7[7];
-    T c9[9], s9[9];
-    T c11[11], s11[11];
-    T c13[13], s13[13];
-    T c16[16], s16[16];
+#define FYG_DECL(r) T c##r[r], s##r[r];
+    FYG_CODELET_TABLES(FYG_DECL)
+#undef FYG_DECL
 };
 
 // One copy per translation unit that launches kernels (no relocatable device code); each such
@@ -186,6 +185,60 @@ template <typename T, typename T2> __device__ __forceinline__ void dft9(T2* a) {
     }
 }
 
+template <int R, typename T> __device__ __forceinline__ const T* kcos() {
+#define FYG_SEL(r) if constexpr (R == r) return kc<T>().c##r; else
+    FYG_CODELET_TABLES(FYG_SEL)
+#undef FYG_SEL
+    return nullptr;
+}
+template <int R, typename T> __device__ __forceinline__ const T* ksin() {
+#define FYG_SEL(r) if constexpr (R == r) return kc<T>().s##r; else
+    FYG_CODELET_TABLES(FYG_SEL)
+#undef FYG_SEL
+    return nullptr;
+}
+
+template <int R, typename T, typename T2> __device__ __forceinline__ void dft(T2* a);
+
+// Composite codelet R = A*B in registers: n = B n1 + n2, k = k1 + A k2.
+// DFT_A over n1, internal twiddle exp(-2 pi i n2 k1 / R), DFT_B over n2; natural-order output.
+template <int A, int B, typename T, typename T2>
+__device__ __forceinline__ void dft_comp(T2* a) {
+    constexpr int R = A * B;
+    const T* C = kcos<R, T>();
+    const T* S = ksin<R, T>();
+    T2 f[B][A];
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) {
+        T2 x[A];
+#pragma unroll
+        for (int n1 = 0; n1 < A; ++n1) x[n1] = a[B * n1 + n2];
+        dft<A, T>(x);
+#pragma unroll
+        for (int k1 = 0; k1 < A; ++k1) f[n2][k1] = x[k1];
+    }
+#pragma unroll
+    for (int n2 = 1; n2 < B; ++n2)
+#pragma unroll
+        for (int k1 = 1; k1 < A; ++k1) {
+            const int e = (n2 * k1) % R;
+            f[n2][k1] = cmul(f[n2][k1], mk<T2>(C[e], -S[e]));
+        }
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) {
+        T2 x[B];
+#pragma unroll
+        for (int n2 = 0; n2 < B; ++n2) x[n2] = f[n2][k1];
+        dft<B, T>(x);
+#pragma unroll
+        for (int k2 = 0; k2 < B; ++k2) a[k1 + A * k2] = x[k2];
+    }
+}
+
+// Stage radices the engine supports (host planner and kernel dispatch share this list).
+#define FYG_STAGE_RADICES(X) \
+    X(2) X(3) X(4) X(5) X(7) X(8) X(9) X(11) X(13) X(16) X(12) X(20) X(24) X(25) X(27) X(32)
+
 template <int R, typename T, typename T2> __device__ __forceinline__ void dft(T2* a) {
     const CodeletConsts<T>& K = kc<T>();
     if constexpr (R == 2) dft2(a);
@@ -198,6 +251,12 @@ template <int R, typename T, typename T2> __device__ __forceinline__ void dft(T2
     else if constexpr (R == 11) dft_odd_prime<11, T>(a, K.c11, K.s11);
     else if constexpr (R == 13) dft_odd_prime<13, T>(a, K.c13, K.s13);
     else if constexpr (R == 16) dft16<T>(a);
+    else if constexpr (R == 12) dft_comp<4, 3, T>(a);
+    else if constexpr (R == 20) dft_comp<4, 5, T>(a);
+    else if constexpr (R == 24) dft_comp<8, 3, T>(a);
+    else if constexpr (R == 25) dft_comp<5, 5, T>(a);
+    else if constexpr (R == 27) dft_comp<3, 9, T>(a);
+    else if constexpr (R == 32) dft_comp<4, 8, T>(a);
 }
 
 }  // namespace fyg

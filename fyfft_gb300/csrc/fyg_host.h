@@ -85,4 +85,12 @@ struct fyg_plan {
     fyg::DevBuf scratch0, scratch1, x0buf, dcbuf, errword;
     fyg::DevBuf stage_in, stage_out;   // staging for host pointers
     size_t stage_in_bytes = 0;
+    // instrumentation: event pairs per launch, accumulated per forward pass
+    bool profile = false;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;
+    std::vector<double> prof_ms;
+    std::vector<int64_t> prof_launches;
+    std::vector<cudaEvent_t> prof_pool;
+    size_t prof_pool_used = 0;
+    ~fyg_plan();
 };

@@ -7,16 +7,15 @@
 
 namespace fyg {
 
-// Tile-pass kernel variants: compute type / input type / output type and the launch bound
-// (MAXT threads per CTA).
+// Tile-pass kernel variants: compute type / input type / output type and radix class; all are
+// launched with at most 512 threads per CTA.
 enum KernelVariant : int {
-    KV_F32_T1024 = 0,   // float  compute, float  I/O
-    KV_F32_T256,
-    KV_F64_T512,        // double compute, double I/O
-    KV_F64_T256,
-    KV_F64_IF32_T512,   // double compute, float in,  double out
-    KV_F64_OF32_T512,   // double compute, double in, float out
-    KV_F64_F32IO_T512,  // double compute, float in,  float out
+    KV_F32_C16 = 0,     // float  compute, float  I/O, stage radices <= 16
+    KV_F32_C32,         // float  compute, float  I/O, stage radices <= 32
+    KV_F64_C16,         // double compute, double I/O
+    KV_F64_IF32_C16,    // double compute, float in,  double out
+    KV_F64_OF32_C16,    // double compute, double in, float out
+    KV_F64_F32IO_C16,   // double compute, float in,  float out
     KV_COUNT
 };
 

@@ -2,8 +2,7 @@
 #include "fyg_k_variant.cuh"
 namespace fyg {
 cudaError_t launch_f64(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st) {
-    if (kv == KV_F64_T512) return launch_variant<double, double, double, 512>(p, grid, threads, smem, st);
-    return launch_variant<double, double, double, 256>(p, grid, threads, smem, st);
+    return launch_variant<double, double, double, 16>(p, grid, threads, smem, st);
 }
 cudaError_t upload_consts_f64(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd) {
     return upload_consts_tu(kf, kd);

@@ -3,9 +3,9 @@
 #include "fyg_k_variant.cuh"
 namespace fyg {
 cudaError_t launch_mixed(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st) {
-    if (kv == KV_F64_IF32_T512) return launch_variant<double, float, double, 512>(p, grid, threads, smem, st);
-    if (kv == KV_F64_OF32_T512) return launch_variant<double, double, float, 512>(p, grid, threads, smem, st);
-    return launch_variant<double, float, float, 512>(p, grid, threads, smem, st);
+    if (kv == KV_F64_IF32_C16) return launch_variant<double, float, double, 16>(p, grid, threads, smem, st);
+    if (kv == KV_F64_OF32_C16) return launch_variant<double, double, float, 16>(p, grid, threads, smem, st);
+    return launch_variant<double, float, float, 16>(p, grid, threads, smem, st);
 }
 cudaError_t upload_consts_mixed(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd) {
     return upload_consts_tu(kf, kd);

@@ -5,10 +5,9 @@
 
 namespace fyg {
 
-template <typename T, typename TI, typename TO, int MAXT>
-cudaError_t launch_variant(const PassParams& p, unsigned grid, int threads, size_t smem,
-                           cudaStream_t st) {
-    auto kern = k_pass<T, TI, TO, MAXT>;
+template <typename T, typename TI, typename TO, int CLASS, bool COLMAJOR>
+cudaError_t launch_layout(const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st) {
+    auto kern = k_pass<T, TI, TO, CLASS, COLMAJOR>;
     constexpr int kMaxDev = 64;
     static size_t smem_set[kMaxDev] = {};
     int dev = 0;
@@ -20,6 +19,12 @@ cudaError_t launch_variant(const PassParams& p, unsigned grid, int threads, size
     }
     kern<<<grid, threads, smem, st>>>(p);
     return cudaGetLastError();
+}
+
+template <typename T, typename TI, typename TO, int CLASS>
+cudaError_t launch_variant(const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st) {
+    if (p.g.colmajor) return launch_layout<T, TI, TO, CLASS, true>(p, grid, threads, smem, st);
+    return launch_layout<T, TI, TO, CLASS, false>(p, grid, threads, smem, st);
 }
 
 // Copies the codelet constants into this translation unit's __constant__ tables.

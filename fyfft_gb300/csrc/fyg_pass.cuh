@@ -15,9 +15,8 @@
 // (src/foye_FFT_mix_radix.hpp:16-83, :536-574) and its radix engines' bit/digit-reversal LUTs:
 // Stockham indexing sorts itself.
 //
-// Inside the CTA the length-R DFT is again a Stockham sweep over radix-r stages; stage 0 loads
-// straight from global memory into registers (coalesced), intermediate stages exchange through
-// shared memory, and the last stage stores straight to global memory.
+// Inside the CTA the length-R DFT is again a Stockham sweep over radix-r stages run in place in
+// shared memory, between a coalesced load phase and a coalesced store phase (fyg_kernels.cuh).
 //
 // Fusions (all selected by uniform runtime fields):
 //   load  LD_PLAIN   x (optionally conjugated)
@@ -46,12 +45,13 @@ struct TileGeom {
     int R;          // in-CTA transform length
     int C;          // columns per tile
     int log2C;      // for the element-major layout (C a power of two)
-    int colmajor;   // 1: smem[c*R + n] (columns are whole contiguous transforms); 0: smem[n*C + c]
+    int colmajor;   // 1: columns are whole contiguous transforms; 0: element-major column tile
     int nst;        // in-CTA stages
     int radix[kMaxStages];
     int twmul[kMaxStages];     // R / (ns * radix): local twiddle exponent multiplier
     FastDiv ns[kMaxStages];    // local Ns before the stage
     FastDiv rr[kMaxStages];    // R / radix (butterflies per column)
+    FastDiv divR;              // R (element index -> column, column-major order)
 };
 
 struct PassParams {
@@ -87,122 +87,78 @@ struct PassParams {
     int* err;                // device error word (bounds violations are recorded, never trapped)
 };
 
-template <typename T> struct ColInfo {
+// Per-column state: the transform b a column belongs to, its column index jj inside the pass,
+// the inter-pass twiddle index k = jj mod Ns, the output column offset and the global bases.
+template <typename T> struct Col {
     int64_t in_base, out_base;
-    int jj, k, out_j, b, valid, pad;
+    int jj, k, out_j, b, valid;
     cplx<T> x0;
 };
 
-// Shared memory: ColInfo[C], then two R*C complex buffers (none when one stage and no mid).
-template <typename T>
-__host__ __device__ inline size_t pass_smem_bytes(int R, int C, int nst, int mid) {
-    const size_t ci = ((size_t)C * sizeof(ColInfo<T>) + 15) & ~(size_t)15;
-    const size_t nbuf = (nst > 1 || mid) ? 2 : 0;
-    return ci + nbuf * (size_t)R * C * sizeof(cplx<T>);
+constexpr int kMaxThreads = 512;
+
+__host__ __device__ inline int colmajor_pitch(int R) { return R + (R >> 4) + 1; }
+
+__host__ __device__ inline size_t tile_elems(int R, int C, int colmajor) {
+    return colmajor ? (size_t)C * colmajor_pitch(R) : (size_t)R * (C + 1);
 }
 
+// Per-column output state kept in shared memory for the store phase.
+template <typename T> struct ColHead {
+    int64_t out_base;
+    int out_j, b, valid, pad;
+    cplx<T> x0;
+};
+
+// Stage schedule copied to shared memory at kernel start (parameter arrays cannot be indexed
+// by a run-time stage number without a local-memory copy).
+struct StageDesc {
+    int radix, twm;
+    FastDiv ns, rr;
+};
+
+template <typename T>
+__host__ __device__ inline size_t tile_head_bytes(int C) {
+    return (((size_t)kMaxStages * sizeof(StageDesc) + (size_t)C * sizeof(ColHead<T>)) + 15) & ~(size_t)15;
+}
+template <typename T>
+__host__ __device__ inline size_t tile_smem_bytes(int R, int C, int colmajor) {
+    return tile_head_bytes<T>(C) + 2 * tile_elems(R, C, colmajor) * sizeof(cplx<T>);
+}
 
 // ---- inter-pass twiddle exp(-2 pi i e / L) from the two-level table ----
-__device__ __forceinline__ float2 tw_two_level(const PassParams& p, uint32_t e, float) {
-    const float4 A = __ldg(reinterpret_cast<const float4*>(p.tw_hi) + (e >> p.tw_shift));
-    const float4 B = __ldg(reinterpret_cast<const float4*>(p.tw_lo) + (e & ((1u << p.tw_shift) - 1)));
+__device__ __forceinline__ float2 tw_two_level(const void* hi, const void* lo, int shift, uint32_t e, float) {
+    const float4 A = __ldg(reinterpret_cast<const float4*>(hi) + (e >> shift));
+    const float4 B = __ldg(reinterpret_cast<const float4*>(lo) + (e & ((1u << shift) - 1)));
     // (Ah + Al)(Bh + Bl) with the small cross terms folded in before the final rounding
     const float cr = fmaf(A.x, B.z, fmaf(-A.y, B.w, fmaf(A.z, B.x, -A.w * B.y)));
     const float ci = fmaf(A.x, B.w, fmaf(A.y, B.z, fmaf(A.z, B.y, A.w * B.x)));
     return make_float2(fmaf(A.x, B.x, fmaf(-A.y, B.y, cr)), fmaf(A.x, B.y, fmaf(A.y, B.x, ci)));
 }
-__device__ __forceinline__ double2 tw_two_level(const PassParams& p, uint32_t e, double) {
-    const double2 A = __ldg(reinterpret_cast<const double2*>(p.tw_hi) + (e >> p.tw_shift));
-    const double2 B = __ldg(reinterpret_cast<const double2*>(p.tw_lo) + (e & ((1u << p.tw_shift) - 1)));
+__device__ __forceinline__ double2 tw_two_level(const void* hi, const void* lo, int shift, uint32_t e, double) {
+    const double2 A = __ldg(reinterpret_cast<const double2*>(hi) + (e >> shift));
+    const double2 B = __ldg(reinterpret_cast<const double2*>(lo) + (e & ((1u << shift) - 1)));
     return cmul(A, B);
 }
 
-template <typename T, typename TI, typename TO>
-struct PassCtx {
+// Column state of global column q of this pass.
+template <typename T, typename TI>
+__device__ __forceinline__ Col<T> make_col(const PassParams& p, int64_t q) {
     using T2 = cplx<T>;
-    using IN2 = cplx<TI>;
-    using OUT2 = cplx<TO>;
-    const PassParams& p;
-    T2* sm;
-    ColInfo<T>* col;
-
-    __device__ __forceinline__ int saddr(int c, int n) const {
-        return p.g.colmajor ? c * p.g.R + n : (n << p.g.log2C) + c;
-    }
-
-    // element n (in-CTA index) of column c, from global memory, with the load fusions
-    __device__ __forceinline__ T2 load(int c, int n) const {
-        const ColInfo<T>& ci = col[c];
-        T2 v = mk<T2>(T(0), T(0));
-        if (!ci.valid) return v;
-        const int64_t gidx = (int64_t)ci.jj + (int64_t)n * p.Rr;
-        const IN2* in = reinterpret_cast<const IN2*>(p.in);
-        if (p.load_mode == LD_PLAIN) {
-            v = to_c(in[ci.in_base + gidx], T());
-        } else if (p.load_mode == LD_CHIRP) {
-            if (gidx < p.nvalid) {
-                v = to_c(in[ci.in_base + gidx], T());
-                if (p.conj_in) v = cconj(v);
-                v = cmul(v, cconj(__ldg(reinterpret_cast<const T2*>(p.chirp) + gidx)));
-            }
-            return v;
-        } else {
-            const int t = __ldg(p.gather + gidx);
-            if (t >= 0) v = to_c(in[ci.in_base + t], T());
-        }
-        if (p.conj_in) v = cconj(v);
-        if (p.Ns > 1 && ci.k != 0 && n != 0) {
-            const uint32_t e = (uint32_t)((uint64_t)n * (uint64_t)ci.k * (uint64_t)p.Lr);
-            v = cmul(v, tw_two_level(p, e, T()));
-        }
-        return v;
-    }
-
-    // element n of column c from shared memory after the forward FFT: * spectrum, conjugate
-    __device__ __forceinline__ T2 load_mid(int c, int n, const T2* src) const {
-        const ColInfo<T>& ci = col[c];
-        T2 v = src[saddr(c, n)];
-        if (!ci.valid) return v;
-        const int64_t gidx = (int64_t)ci.jj + (int64_t)n * p.Rr;
-        if (p.dc_capture && gidx == 0) {
-            // Rader: the DC term of the forward convolution FFT is sum_{n>=1} x[n]
-            reinterpret_cast<T2*>(p.dcbuf)[ci.b] = v;
-        }
-        v = cmul(v, __ldg(reinterpret_cast<const T2*>(p.spectrum) + gidx));
-        return cconj(v);
-    }
-
-    __device__ __forceinline__ void store(int c, int n, T2 v) const {
-        const ColInfo<T>& ci = col[c];
-        if (!ci.valid) return;
-        const int64_t oidx = (int64_t)ci.out_j + (int64_t)n * p.Ns_out;
-        OUT2* out = reinterpret_cast<OUT2*>(p.out);
-        if (p.store_mode == ST_PLAIN) {
-            if (p.conj_out) v = cconj(v);
-            v = cscale(v, (T)p.scale);
-            out[ci.out_base + oidx] = to_c(v, TO());
-        } else if (p.store_mode == ST_CHIRP) {
-            if (oidx < p.nvalid) {
-                v = cscale(cmul(__ldg(reinterpret_cast<const T2*>(p.chirp) + oidx), v), (T)p.scale);
-                if (p.conj_out) v = cconj(v);
-                out[ci.out_base + oidx] = to_c(v, TO());
-            }
-        } else {
-            const T s2 = (T)p.scale2;
-            if (oidx == 0) {
-                // DC: (x0 + A0) forward, (x0 + conj(A0)) inverse; A0 saved by the mid pass
-                T2 a0 = reinterpret_cast<const T2*>(p.dcbuf)[ci.b];
-                if (!p.conj_out) a0 = cconj(a0);
-                out[ci.out_base] = to_c(cscale(cadd(ci.x0, a0), s2), TO());
-            }
-            const int t = __ldg(p.scatter + oidx);
-            if (t > 0) {
-                v = cscale(v, (T)p.scale);
-                if (p.conj_out) v = cconj(v);
-                out[ci.out_base + t] = to_c(cscale(cadd(ci.x0, v), s2), TO());
-            }
-        }
-    }
-};
+    Col<T> ci;
+    ci.valid = q < p.ncols;
+    const uint32_t qq = (uint32_t)(ci.valid ? q : 0);
+    const uint32_t b = p.div_Rr.div(qq);
+    const uint32_t jj = qq - b * (uint32_t)p.Rr;
+    ci.b = (int)b;
+    ci.jj = (int)jj;
+    ci.k = (int)(jj - p.div_Ns.div(jj) * (uint32_t)p.Ns);
+    const uint32_t qo = p.div_Ns_out.div(jj);
+    ci.out_j = (int)(qo * (uint32_t)p.Ns_out * (uint32_t)p.g.R + (jj - qo * (uint32_t)p.Ns_out));
+    ci.in_base = (int64_t)b * p.idist;
+    ci.out_base = (int64_t)b * p.odist;
+    ci.x0 = mk<T2>(T(0), T(0));
+    return ci;
+}
 
 }  // namespace fyg

@@ -30,24 +30,20 @@
 namespace fyg {
 
 cudaError_t launch_f32(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st);
+cudaError_t launch_f32c32(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st);
 cudaError_t launch_f64(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st);
 cudaError_t launch_mixed(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st);
 cudaError_t launch_scale_copy(const void* in, void* out, size_t n, int dtype, double scale, int conj,
                               cudaStream_t st);
 
 VariantInfo variant_info(int kv) {
-    switch (kv) {
-        case KV_F32_T1024: return {1024, 8};
-        case KV_F32_T256: return {256, 8};
-        case KV_F64_T512: return {512, 16};
-        case KV_F64_T256: return {256, 16};
-        default: return {512, 16};
-    }
+    return {512, (kv == KV_F32_C16 || kv == KV_F32_C32) ? 8 : 16};
 }
 
 cudaError_t launch_pass(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st) {
-    if (kv == KV_F32_T1024 || kv == KV_F32_T256) return launch_f32(kv, p, grid, threads, smem, st);
-    if (kv == KV_F64_T512 || kv == KV_F64_T256) return launch_f64(kv, p, grid, threads, smem, st);
+    if (kv == KV_F32_C16) return launch_f32(kv, p, grid, threads, smem, st);
+    if (kv == KV_F32_C32) return launch_f32c32(kv, p, grid, threads, smem, st);
+    if (kv == KV_F64_C16) return launch_f64(kv, p, grid, threads, smem, st);
     return launch_mixed(kv, p, grid, threads, smem, st);
 }
 
@@ -174,50 +170,87 @@ static int ref_strategy(uint64_t n) {
 // ------------------------------------------------------------------------------------------
 
 constexpr size_t kSmemLimit = 232448;  // 227 KB dynamic shared memory per CTA on sm_100/103
-constexpr int kMultiC = 8;             // columns per tile in multi-pass: 8 x 8 B = 64 B segments (fp32)
 
-template <typename T> static size_t colinfo_sz() { return sizeof(ColInfo<T>); }
-
-static size_t smem_for(int cb, int R, int C, int nst, int mid) {
-    return cb == 8 ? pass_smem_bytes<float>(R, C, nst, mid) : pass_smem_bytes<double>(R, C, nst, mid);
+static size_t smem_for(int cb, int R, int C, bool colmajor) {
+    return cb == 8 ? tile_smem_bytes<float>(R, C, colmajor) : tile_smem_bytes<double>(R, C, colmajor);
 }
 
-// radix schedule of an in-CTA transform of length R (13-smooth); empty if not representable
-static std::vector<int> radices_for(int R) {
-    std::vector<int> r;
-    int n = R, a = 0, b = 0;
-    while (n % 2 == 0) { n /= 2; ++a; }
-    while (n % 3 == 0) { n /= 3; ++b; }
-    std::vector<int> odd;
-    for (int p : {5, 7, 11, 13})
-        while (n % p == 0) { n /= p; odd.push_back(p); }
-    if (n != 1) return {};
-    while (a >= 4) { r.push_back(16); a -= 4; }
-    if (a == 3) r.push_back(8);
-    if (a == 2) r.push_back(4);
-    if (a == 1) r.push_back(2);
-    while (b >= 2) { r.push_back(9); b -= 2; }
-    if (b == 1) r.push_back(3);
-    for (int p : odd) r.push_back(p);
-    if (r.size() > (size_t)kMaxStages) return {};
-    return r;
-}
+static int tile_class(int cb, int rmax) { return (cb == 8 && rmax > 16) ? 32 : 16; }
 
-static int max_single_R(int cb) {
-    // two ping-pong buffers of R complex plus one ColInfo
-    return (int)((kSmemLimit - 64) / (2 * (size_t)cb));
-}
+// Stage radices the kernels implement (FYG_STAGE_RADICES), and the largest one per compute type
+// (a radix-r butterfly keeps 2r values in registers).
+static const int kRadices[] = {
+#define FYG_LIST(r) r,
+    FYG_STAGE_RADICES(FYG_LIST)
+#undef FYG_LIST
+};
+static int max_radix(int cb) { return cb == 8 ? 32 : 16; }
 
-static int max_multi_R(int cb) {
-    return (int)((kSmemLimit - kMultiC * 64) / (2 * (size_t)cb * kMultiC));
-}
-
-// Split L into P >= 2 pass radices, each <= Rmax and representable; fewest passes, then fewest
-// in-CTA stages, then the most balanced split.
-static bool split_passes(uint64_t L, int Rmax, std::vector<int>& out) {
+// Radix schedule of an in-CTA transform of length R: fewest stages, then the smallest largest
+// radix (register pressure), then larger radices first.  Empty if R is not representable.
+static std::vector<int> radices_for(int R, int cb = 8) {
+    static std::mutex mu;
+    static std::map<std::pair<int, int>, std::vector<int>> memo;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = memo.find({R, cb});
+        if (it != memo.end()) return it->second;
+    }
+    const int rmax = max_radix(cb);
+    // best[d] = (stages, largest radix) for every divisor d of R
+    std::map<int, std::pair<int, int>> best;
+    std::map<int, int> choice;
     std::vector<int> divs;
-    for (int d = 4; d <= Rmax && (uint64_t)d <= L; ++d)
-        if (L % d == 0 && !radices_for(d).empty()) divs.push_back(d);
+    for (int d = 1; d <= R; ++d) if (R % d == 0) divs.push_back(d);
+    best[1] = {0, 0};
+    for (int d : divs) {
+        if (d == 1) continue;
+        std::pair<int, int> bd = {1 << 20, 0};
+        int bc = 0;
+        for (int r : kRadices) {
+            if (r > rmax || d % r) continue;
+            auto it = best.find(d / r);
+            if (it == best.end() || it->second.first >= (1 << 20)) continue;
+            std::pair<int, int> cand = {it->second.first + 1, std::max(it->second.second, r)};
+            if (cand < bd || (cand == bd && r > bc)) { bd = cand; bc = r; }
+        }
+        best[d] = bd;
+        choice[d] = bc;
+    }
+    std::vector<int> out;
+    if (best[R].first < (1 << 20) && best[R].first <= kMaxStages) {
+        for (int d = R; d > 1; d /= choice[d]) out.push_back(choice[d]);
+        std::sort(out.begin(), out.end(), std::greater<int>());
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    memo[{R, cb}] = out;
+    return out;
+}
+
+// Columns per element-major tile: 8 (64 B fp32 segments) while two CTAs still fit on an SM,
+// else 4; 0 if not even 4 columns fit.
+static bool tile_fits(int cb, int R, int C, bool colmajor);
+static int multi_C(int cb, int R) {
+    if (tile_fits(cb, R, 8, false) && smem_for(cb, R, 8, false) <= kSmemLimit / 2) return 8;
+    if (tile_fits(cb, R, 4, false)) return 4;
+    return 0;
+}
+
+static bool tile_fits(int cb, int R, int C, bool colmajor) {
+    const std::vector<int> r = radices_for(R, cb);
+    if (r.empty()) return false;
+    return smem_for(cb, R, C, colmajor) <= kSmemLimit;
+}
+
+// Split L into P >= 2 pass radices whose C-column tiles fit in shared memory: fewest passes,
+// then fewest in-CTA stages, then the most balanced split.  For convolution pipelines the last
+// forward radix also runs the fused mid pass (two buffers).
+static bool split_passes(uint64_t L, int cb, bool conv, std::vector<int>& out) {
+    std::vector<int> divs;
+    for (int d = 4; d <= 4096 && (uint64_t)d <= L; ++d)
+        if (L % d == 0 && multi_C(cb, d)) divs.push_back(d);
+    if (divs.empty()) return false;
+    const int Rmax = divs.back();
     for (int P = 2; P <= 6; ++P) {
         double best = 1e30;
         std::vector<int> best_f, cur;
@@ -225,20 +258,20 @@ static bool split_passes(uint64_t L, int Rmax, std::vector<int>& out) {
         std::function<void(uint64_t, int)> rec = [&](uint64_t rem, int left) {
             if (left == 1) {
                 if (rem > (uint64_t)Rmax || rem < 2) return;
-                std::vector<int> rr = radices_for((int)rem);
-                if (rr.empty()) return;
+                if (!multi_C(cb, (int)rem)) return;
                 cur.push_back((int)rem);
-                double cost = 0;
-                for (int f : cur) cost += (double)radices_for(f).size() + 0.25 * std::fabs(std::log((double)f) - target);
-                if (cost < best) { best = cost; best_f = cur; }
+                {
+                    double cost = 0;
+                    for (int f : cur)
+                        cost += (double)radices_for(f, cb).size() + 0.25 * std::fabs(std::log((double)f) - target);
+                    if (cost < best) { best = cost; best_f = cur; }
+                }
                 cur.pop_back();
                 return;
             }
             for (int d : divs) {
                 if (rem % d) continue;
-                // remaining must fit in left-1 passes
-                double cap = std::pow((double)Rmax, left - 1);
-                if ((double)(rem / d) > cap) continue;
+                if ((double)(rem / d) > std::pow((double)Rmax, left - 1)) continue;
                 cur.push_back(d);
                 rec(rem / d, left - 1);
                 cur.pop_back();
@@ -246,7 +279,6 @@ static bool split_passes(uint64_t L, int Rmax, std::vector<int>& out) {
         };
         rec(L, P);
         if (!best_f.empty()) {
-            // larger radices first: the first pass writes fully contiguous R-runs
             out = best_f;
             return true;
         }
@@ -271,6 +303,7 @@ static void fill_geom(TileGeom& g, int R, int C, bool colmajor, const std::vecto
         g.rr[s] = make_fastdiv((uint32_t)(R / rad[s]));
         ns *= rad[s];
     }
+    g.divR = make_fastdiv((uint32_t)R);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -366,14 +399,15 @@ struct PipeSpec {
     int C;                    // columns per tile (single-pass: transforms per CTA)
 };
 
-static int pick_variant(int compute_cb, int tin_cb, int tout_cb, int threads) {
-    if (compute_cb == 8) return threads <= 256 ? KV_F32_T256 : KV_F32_T1024;
-    if (tin_cb == 16 && tout_cb == 16) return threads <= 256 ? KV_F64_T256 : KV_F64_T512;
-    if (tin_cb == 8 && tout_cb == 16) return KV_F64_IF32_T512;
-    if (tin_cb == 16 && tout_cb == 8) return KV_F64_OF32_T512;
-    return KV_F64_F32IO_T512;
+static int pick_variant(int compute_cb, int tin_cb, int tout_cb, int cls) {
+    if (compute_cb == 8) return cls <= 16 ? KV_F32_C16 : KV_F32_C32;
+    if (tin_cb == 16 && tout_cb == 16) return KV_F64_C16;
+    if (tin_cb == 8 && tout_cb == 16) return KV_F64_IF32_C16;
+    if (tin_cb == 16 && tout_cb == 8) return KV_F64_OF32_C16;
+    return KV_F64_F32IO_C16;
 }
 
+// about 16 elements per thread
 static int threads_for(int R, int C, int maxt) {
     int t = (R * C + 15) / 16;
     t = (t + 31) / 32 * 32;
@@ -405,8 +439,8 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
         else { R = ps.prad[K - 1 - i]; Ns = ns_inv; ns_inv *= R; }
         if (mid) ns_inv = R;  // the mid pass also performs the first inverse pass (radix R, Ns 1)
         const bool single = (P == 1);
-        const int C = single ? ps.C : kMultiC;
-        const std::vector<int> rad = radices_for(R);
+        const int C = single ? ps.C : multi_C(cb, R);
+        const std::vector<int> rad = radices_for(R, cb);
         fill_geom(p.g, R, C, single, rad);
         p.Rr = (int)(L / R);
         p.Ns = (int)Ns;
@@ -458,11 +492,11 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
                 p.scale = inverse ? 1.0 / (double)n : 1.0;
             }
         }
-        const int maxt = cb == 8 ? 1024 : 512;
-        d.threads = threads_for(R, C, maxt);
-        d.kv = pick_variant(cb, (int)d.in_elem_bytes, (int)d.out_elem_bytes, d.threads);
-        d.threads = std::min(d.threads, variant_info(d.kv).maxt);
-        d.smem = smem_for(cb, R, C, (int)rad.size(), p.mid);
+        const int rmax = *std::max_element(rad.begin(), rad.end());
+        const int cls = tile_class(cb, rmax);
+        d.threads = threads_for(R, C, kMaxThreads);
+        d.kv = pick_variant(cb, (int)d.in_elem_bytes, (int)d.out_elem_bytes, cls);
+        d.smem = smem_for(cb, R, C, single);
         if (d.smem > kSmemLimit)
             return set_error(FYG_ERR_UNSUPPORTED, "tile of " + std::to_string(R) + "x" + std::to_string(C) +
                                                       " exceeds shared memory");
@@ -492,8 +526,7 @@ static int make_plan(fyg_plan* pl) {
         return FYG_OK;
     }
     // ---- strategy ----
-    const int single_cap_io = max_single_R(io_cb);
-    if (is_smooth(n, 13) && n <= (uint64_t)single_cap_io && !radices_for((int)n).empty()) {
+    if (is_smooth(n, 13) && n <= 16384 && tile_fits(io_cb, (int)n, 1, true)) {
         ps.kind = GS_SINGLE;
         ps.L = n;
         ps.prad = {(int)n};
@@ -518,9 +551,9 @@ static int make_plan(fyg_plan* pl) {
     pl->compute_bytes = (pl->dtype == FYG_C64 || pl->conv_fp64) ? 16 : 8;
     const int cb = pl->compute_bytes;
     if (ps.kind != GS_SINGLE) {
-        if (conv && ps.L <= (uint64_t)max_single_R(cb) && !radices_for((int)ps.L).empty()) {
+        if (conv && ps.L <= 16384 && tile_fits(cb, (int)ps.L, 1, true)) {
             ps.prad = {(int)ps.L};
-        } else if (!split_passes(ps.L, max_multi_R(cb), ps.prad)) {
+        } else if (!split_passes(ps.L, cb, conv, ps.prad)) {
             return set_error(FYG_ERR_UNSUPPORTED, "no pass decomposition for length " + std::to_string(ps.L));
         }
     }
@@ -693,8 +726,25 @@ static int run_pipeline(fyg_plan* pl, const std::vector<PassDesc>& pipe, const v
                 else p.scale *= final_scale_mul;
             }
             const unsigned grid = (unsigned)((p.ncols + p.g.C - 1) / p.g.C);
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (pl->profile && &pipe == &pl->fwd) {
+                if (pl->prof_pool_used + 2 > pl->prof_pool.size()) {
+                    for (int k = 0; k < 64; ++k) {
+                        cudaEvent_t ev;
+                        if (cudaEventCreate(&ev) != cudaSuccess) return cuda_error(cudaGetLastError(), "event");
+                        pl->prof_pool.push_back(ev);
+                    }
+                }
+                e0 = pl->prof_pool[pl->prof_pool_used++];
+                e1 = pl->prof_pool[pl->prof_pool_used++];
+                cudaEventRecord(e0, st);
+            }
             cudaError_t e = launch_pass(d.kv, p, grid, d.threads, d.smem, st);
             if (e != cudaSuccess) return cuda_error(e, "tile pass launch");
+            if (e0) {
+                cudaEventRecord(e1, st);
+                pl->prof_pending.push_back({(int)i, {e0, e1}});
+            }
         }
     }
     return FYG_OK;
@@ -781,6 +831,10 @@ static int gpu_fft_f64(size_t n, const std::vector<double2>& h, std::vector<doub
 
 using namespace fyg;
 
+fyg_plan::~fyg_plan() {
+    for (cudaEvent_t e : prof_pool) cudaEventDestroy(e);
+}
+
 extern "C" {
 
 int fyg_plan_create(size_t n, int dtype, size_t batch, int flags, fyg_plan** out) {
@@ -813,6 +867,59 @@ int fyg_plan_create(size_t n, int dtype, size_t batch, int flags, fyg_plan** out
 
 int fyg_plan_destroy(fyg_plan* plan) {
     delete plan;
+    return FYG_OK;
+}
+
+int fyg_plan_launches(const fyg_plan* plan, int* launches) {
+    if (!plan || !launches) return set_error(FYG_ERR_NULL_PTR, "null argument");
+    const size_t chunks = (plan->batch + plan->chunk - 1) / plan->chunk;
+    *launches = plan->strategy == GS_COPY ? 1 : (int)(plan->fwd.size() * chunks);
+    return FYG_OK;
+}
+
+int fyg_plan_profile(fyg_plan* plan, int enable) {
+    if (!plan) return set_error(FYG_ERR_NULL_PTR, "null plan");
+    plan->profile = enable != 0;
+    plan->prof_ms.assign(plan->fwd.size(), 0.0);
+    plan->prof_launches.assign(plan->fwd.size(), 0);
+    plan->prof_pending.clear();
+    plan->prof_pool_used = 0;
+    return FYG_OK;
+}
+
+int fyg_plan_profile_read(fyg_plan* plan, double* total_ms, int64_t* launches, int64_t* bytes_per_launch,
+                          int max_passes, int* n_passes) {
+    if (!plan) return set_error(FYG_ERR_NULL_PTR, "null plan");
+    const int np = (int)plan->fwd.size();
+    if (plan->prof_ms.size() != (size_t)np) {
+        plan->prof_ms.assign(np, 0.0);
+        plan->prof_launches.assign(np, 0);
+    }
+    for (auto& pe : plan->prof_pending) {
+        cudaError_t e = cudaEventSynchronize(pe.second.second);
+        if (e != cudaSuccess) return cuda_error(e, "profile event");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, pe.second.first, pe.second.second);
+        plan->prof_ms[pe.first] += ms;
+        plan->prof_launches[pe.first] += 1;
+    }
+    plan->prof_pending.clear();
+    plan->prof_pool_used = 0;
+    const int io_cb = plan->dtype == FYG_C32 ? 8 : 16;
+    for (int i = 0; i < np && i < max_passes; ++i) {
+        const PassDesc& d = plan->fwd[i];
+        // elements one launch reads and writes: a full sweep of the chunk's transforms, counted
+        // at the length actually stored on each side (N for user buffers, L for scratch)
+        const int64_t nb = (int64_t)plan->chunk;
+        const int64_t rd = d.in_role == ROLE_IN ? (int64_t)plan->n : (int64_t)plan->L;
+        const int64_t wr = d.out_role == ROLE_OUT ? (int64_t)plan->n : (int64_t)plan->L;
+        if (total_ms) total_ms[i] = plan->prof_ms[i];
+        if (launches) launches[i] = plan->prof_launches[i];
+        if (bytes_per_launch)
+            bytes_per_launch[i] = nb * (rd * (d.in_role == ROLE_IN ? io_cb : plan->compute_bytes) +
+                                        wr * (d.out_role == ROLE_OUT ? io_cb : plan->compute_bytes));
+    }
+    if (n_passes) *n_passes = np;
     return FYG_OK;
 }
 

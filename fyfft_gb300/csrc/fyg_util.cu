@@ -13,6 +13,7 @@ namespace fyg {
 cudaError_t upload_consts_f32(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd);
 cudaError_t upload_consts_f64(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd);
 cudaError_t upload_consts_mixed(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd);
+cudaError_t upload_consts_f32c32(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd);
 
 namespace {
 
@@ -26,13 +27,9 @@ void fill_consts(CodeletConsts<T>& K) {
             s[m] = (T)sinl(a);
         }
     };
-    put(K.c3, K.s3, 3);
-    put(K.c5, K.s5, 5);
-    put(K.c7, K.s7, 7);
-    put(K.c9, K.s9, 9);
-    put(K.c11, K.s11, 11);
-    put(K.c13, K.s13, 13);
-    put(K.c16, K.s16, 16);
+#define FYG_PUT(r) put(K.c##r, K.s##r, r);
+    FYG_CODELET_TABLES(FYG_PUT)
+#undef FYG_PUT
 }
 
 std::mutex g_init_mu;
@@ -53,6 +50,7 @@ cudaError_t ensure_device_constants() {
     e = upload_consts_f32(kf, kd);
     if (e == cudaSuccess) e = upload_consts_f64(kf, kd);
     if (e == cudaSuccess) e = upload_consts_mixed(kf, kd);
+    if (e == cudaSuccess) e = upload_consts_f32c32(kf, kd);
     if (e == cudaSuccess && dev < 128) g_dev_init[dev] = true;
     return e;
 }

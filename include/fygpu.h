@@ -89,6 +89,18 @@ int fyg_gpu_strategy(size_t n);
  * passes per direction, and the GPU strategy. */
 int fyg_plan_info(const fyg_plan* plan, size_t* conv_length, int* passes, int* strategy);
 
+/* Kernel launches one fyg_execute of this plan issues (passes x L2 chunks). */
+int fyg_plan_launches(const fyg_plan* plan, int* launches);
+
+/* Instrumentation (no counterpart in the reference): when enabled, every pass launch of
+ * fyg_execute is bracketed by CUDA events on the execution stream and its duration is
+ * accumulated per pass.  fyg_plan_profile_read synchronizes, then reports for each of up to
+ * max_passes passes of the forward pipeline: total milliseconds, launch count and the
+ * algorithmic bytes one launch moves (elements read + elements written, times element size). */
+int fyg_plan_profile(fyg_plan* plan, int enable);
+int fyg_plan_profile_read(fyg_plan* plan, double* total_ms, int64_t* launches, int64_t* bytes_per_launch,
+                          int max_passes, int* n_passes);
+
 /* Uneven batch: `count` transforms with the given lengths, packed back to back (element
  * offsets given at execute time).  One persistent kernel runs them all from a device work
  * queue.  No counterpart in the reference (it runs one transform per call). */
