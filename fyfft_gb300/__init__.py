@@ -35,7 +35,8 @@ EXPORTED_SYMBOLS = (
     "fyg_plan_create", "fyg_plan_destroy", "fyg_execute", "fyg_execute_adjoint", "fyg_strategy",
     "fyg_gpu_strategy", "fyg_plan_info", "fyg_plan_launches", "fyg_plan_profile",
     "fyg_plan_profile_read", "fyg_batch_create", "fyg_batch_destroy",
-    "fyg_batch_execute", "fyg_batch_execute_plain", "fyg_last_error_string", "fyg_fill_random",
+    "fyg_batch_execute", "fyg_batch_execute_plain", "fyg_execute_noalloc", "fyg_last_error_string",
+    "fyg_fill_random",
     "fyg_fill_random_device", "fyg_version",
 )
 
@@ -81,6 +82,7 @@ def lib() -> ctypes.CDLL:
         L.fyg_batch_destroy.argtypes = [vp]
         L.fyg_batch_execute.argtypes = [vp, vp, vp, vp, i, vp]
         L.fyg_batch_execute_plain.argtypes = [vp, vp, vp, i, vp]
+        L.fyg_execute_noalloc.argtypes = [sz, sz, i, i, vp, vp, vp]
         L.fyg_last_error_string.restype = ctypes.c_char_p
         L.fyg_fill_random.argtypes = [u64, i, i, sz, vp]
         L.fyg_fill_random_device.argtypes = [u64, i, i, sz, vp, vp]

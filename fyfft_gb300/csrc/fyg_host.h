@@ -20,6 +20,21 @@ void fill_random_host(uint64_t seed, int dist, int dtype, size_t n, void* out);
 
 FastDiv make_fastdiv(uint32_t d);
 
+// Planner building blocks (fyg_plan.cu), shared with the allocation-free entry point.
+bool is_smooth(uint64_t n, uint64_t b);
+std::vector<int> radices_for(int R, int cb = 8);
+bool tile_fits(int cb, int R, int C, bool colmajor);
+int multi_C(int cb, int R);
+bool split_passes(uint64_t L, int cb, bool conv, std::vector<int>& out);
+void fill_geom(TileGeom& g, int R, int C, bool colmajor, const std::vector<int>& rad);
+size_t smem_for(int cb, int R, int C, bool colmajor);
+int tile_class(int cb, int rmax);
+int pick_variant(int compute_cb, int tin_cb, int tout_cb, int cls);
+int threads_for(int R, int C, int maxt);
+void twiddle_ld(uint64_t t, uint64_t n, long double* c, long double* s);
+std::vector<unsigned char> host_local_table(int R, int cb);
+void host_two_level(uint64_t L, int cb, std::vector<unsigned char>& hi, std::vector<unsigned char>& lo, int* shift);
+
 // GPU-side strategy of a plan (what actually runs).
 enum GpuStrategy : int {
     GS_SINGLE = 0,      // one tile pass (whole transform in one CTA)

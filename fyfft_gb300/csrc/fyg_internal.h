@@ -29,6 +29,9 @@ cudaError_t launch_pass(int kv, const PassParams& p, unsigned grid, int threads,
 // Uploads the codelet constant tables to the current device (once per device).
 cudaError_t ensure_device_constants();
 
+// Host values of the codelet constant tables (for translation units that upload their own).
+void codelet_consts(CodeletConsts<float>* kf, CodeletConsts<double>* kd);
+
 // Device RNG fill (fyg_fill_random_device).
 cudaError_t launch_fill_random(uint64_t seed, int dist, int dtype, size_t n, void* out,
                                cudaStream_t st);

@@ -5,9 +5,9 @@
 
 namespace fyg {
 
-template <typename T, typename TI, typename TO, int CLASS, bool COLMAJOR>
+template <typename T, typename TI, typename TO, int CLASS, bool COLMAJOR, int TAG = 0>
 cudaError_t launch_layout(const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st) {
-    auto kern = k_pass<T, TI, TO, CLASS, COLMAJOR>;
+    auto kern = k_pass<T, TI, TO, CLASS, COLMAJOR, TAG>;
     constexpr int kMaxDev = 64;
     static size_t smem_set[kMaxDev] = {};
     int dev = 0;
@@ -21,10 +21,10 @@ cudaError_t launch_layout(const PassParams& p, unsigned grid, int threads, size_
     return cudaGetLastError();
 }
 
-template <typename T, typename TI, typename TO, int CLASS>
+template <typename T, typename TI, typename TO, int CLASS, int TAG = 0>
 cudaError_t launch_variant(const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st) {
-    if (p.g.colmajor) return launch_layout<T, TI, TO, CLASS, true>(p, grid, threads, smem, st);
-    return launch_layout<T, TI, TO, CLASS, false>(p, grid, threads, smem, st);
+    if (p.g.colmajor) return launch_layout<T, TI, TO, CLASS, true, TAG>(p, grid, threads, smem, st);
+    return launch_layout<T, TI, TO, CLASS, false, TAG>(p, grid, threads, smem, st);
 }
 
 // Copies the codelet constants into this translation unit's __constant__ tables.

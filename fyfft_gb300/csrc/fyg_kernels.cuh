@@ -383,7 +383,8 @@ __device__ __forceinline__ void store_flat_plain(const PassParams& p, const cplx
 // ------------------------------------------------------------------------------------------
 // The kernel
 // ------------------------------------------------------------------------------------------
-template <typename T, typename TI, typename TO, int CLASS, bool COLMAJOR>
+// TAG only distinguishes instantiations made by different translation units.
+template <typename T, typename TI, typename TO, int CLASS, bool COLMAJOR, int TAG = 0>
 __global__ void __launch_bounds__(kMaxThreads) k_pass(const __grid_constant__ PassParams p) {
     extern __shared__ __align__(16) unsigned char smraw[];
     using T2 = cplx<T>;

@@ -133,7 +133,7 @@ static uint64_t max_prime_factor(uint64_t n) {
     return best;
 }
 
-static bool is_smooth(uint64_t n, uint64_t b) { return n >= 1 && max_prime_factor(n) <= b; }
+bool is_smooth(uint64_t n, uint64_t b) { return n >= 1 && max_prime_factor(n) <= b; }
 
 static uint64_t next_smooth7(uint64_t n) {
     for (uint64_t m = std::max<uint64_t>(n, 1);; ++m)
@@ -171,11 +171,11 @@ static int ref_strategy(uint64_t n) {
 
 constexpr size_t kSmemLimit = 232448;  // 227 KB dynamic shared memory per CTA on sm_100/103
 
-static size_t smem_for(int cb, int R, int C, bool colmajor) {
+size_t smem_for(int cb, int R, int C, bool colmajor) {
     return cb == 8 ? tile_smem_bytes<float>(R, C, colmajor) : tile_smem_bytes<double>(R, C, colmajor);
 }
 
-static int tile_class(int cb, int rmax) { return (cb == 8 && rmax > 16) ? 32 : 16; }
+int tile_class(int cb, int rmax) { return (cb == 8 && rmax > 16) ? 32 : 16; }
 
 // Stage radices the kernels implement (FYG_STAGE_RADICES), and the largest one per compute type
 // (a radix-r butterfly keeps 2r values in registers).
@@ -188,7 +188,7 @@ static int max_radix(int cb) { return cb == 8 ? 32 : 16; }
 
 // Radix schedule of an in-CTA transform of length R: fewest stages, then the smallest largest
 // radix (register pressure), then larger radices first.  Empty if R is not representable.
-static std::vector<int> radices_for(int R, int cb = 8) {
+std::vector<int> radices_for(int R, int cb) {
     static std::mutex mu;
     static std::map<std::pair<int, int>, std::vector<int>> memo;
     {
@@ -229,14 +229,13 @@ static std::vector<int> radices_for(int R, int cb = 8) {
 
 // Columns per element-major tile: 8 (64 B fp32 segments) while two CTAs still fit on an SM,
 // else 4; 0 if not even 4 columns fit.
-static bool tile_fits(int cb, int R, int C, bool colmajor);
-static int multi_C(int cb, int R) {
+int multi_C(int cb, int R) {
     if (tile_fits(cb, R, 8, false) && smem_for(cb, R, 8, false) <= kSmemLimit / 2) return 8;
     if (tile_fits(cb, R, 4, false)) return 4;
     return 0;
 }
 
-static bool tile_fits(int cb, int R, int C, bool colmajor) {
+bool tile_fits(int cb, int R, int C, bool colmajor) {
     const std::vector<int> r = radices_for(R, cb);
     if (r.empty()) return false;
     return smem_for(cb, R, C, colmajor) <= kSmemLimit;
@@ -245,7 +244,7 @@ static bool tile_fits(int cb, int R, int C, bool colmajor) {
 // Split L into P >= 2 pass radices whose C-column tiles fit in shared memory: fewest passes,
 // then fewest in-CTA stages, then the most balanced split.  For convolution pipelines the last
 // forward radix also runs the fused mid pass (two buffers).
-static bool split_passes(uint64_t L, int cb, bool conv, std::vector<int>& out) {
+bool split_passes(uint64_t L, int cb, bool conv, std::vector<int>& out) {
     std::vector<int> divs;
     for (int d = 4; d <= 4096 && (uint64_t)d <= L; ++d)
         if (L % d == 0 && multi_C(cb, d)) divs.push_back(d);
@@ -286,7 +285,7 @@ static bool split_passes(uint64_t L, int cb, bool conv, std::vector<int>& out) {
     return false;
 }
 
-static void fill_geom(TileGeom& g, int R, int C, bool colmajor, const std::vector<int>& rad) {
+void fill_geom(TileGeom& g, int R, int C, bool colmajor, const std::vector<int>& rad) {
     std::memset(&g, 0, sizeof(g));
     g.R = R;
     g.C = C;
@@ -313,7 +312,7 @@ static void fill_geom(TileGeom& g, int R, int C, bool colmajor, const std::vecto
 static const long double kTwoPiL = 6.283185307179586476925286766559005768L;
 
 // exp(-2 pi i t/n) in long double with exact integer reduction of t
-static void twiddle_ld(uint64_t t, uint64_t n, long double* c, long double* s) {
+void twiddle_ld(uint64_t t, uint64_t n, long double* c, long double* s) {
     t %= n;
     // reduce to the first octant-friendly form: angle = 2 pi t / n, t < n
     const long double a = kTwoPiL * (long double)t / (long double)n;
@@ -321,61 +320,62 @@ static void twiddle_ld(uint64_t t, uint64_t n, long double* c, long double* s) {
     *s = -sinl(a);
 }
 
+// Host images of the twiddle tables (shared by plans and by the allocation-free entry point).
+std::vector<unsigned char> host_local_table(int R, int cb) {
+    std::vector<unsigned char> out((size_t)R * 2 * cb);
+    for (int t = 0; t < R; ++t) {
+        long double c, s;
+        twiddle_ld(t, R, &c, &s);
+        if (cb == 8) reinterpret_cast<float2*>(out.data())[t] = make_float2((float)c, (float)s);
+        else reinterpret_cast<double2*>(out.data())[t] = make_double2((double)c, (double)s);
+    }
+    return out;
+}
+
+// two-level table of w_L: hi[i] = w^(i 2^s), lo[j] = w^j; float tables hold (hi, lo) pairs
+void host_two_level(uint64_t L, int cb, std::vector<unsigned char>& hi, std::vector<unsigned char>& lo, int* shift) {
+    int s = 0;
+    while ((1ull << (2 * s)) < L) ++s;  // 2^s ~ sqrt(L)
+    if (s < 1) s = 1;
+    const uint64_t B = 1ull << s, nhi = (L + B - 1) / B;
+    auto pack = [](long double c, long double sn) {
+        const float ch = (float)c, sh = (float)sn;
+        return make_float4(ch, sh, (float)(c - (long double)ch), (float)(sn - (long double)sh));
+    };
+    const size_t es = cb == 8 ? sizeof(float4) : sizeof(double2);
+    hi.assign(nhi * es, 0);
+    lo.assign(B * es, 0);
+    for (uint64_t i = 0; i < nhi + B; ++i) {
+        const bool h = i < nhi;
+        const uint64_t t = h ? i * B : i - nhi;
+        long double c, sn;
+        twiddle_ld(t, L, &c, &sn);
+        unsigned char* dst = h ? hi.data() + i * es : lo.data() + (i - nhi) * es;
+        if (cb == 8) *reinterpret_cast<float4*>(dst) = pack(c, sn);
+        else *reinterpret_cast<double2*>(dst) = make_double2((double)c, (double)sn);
+    }
+    *shift = s;
+}
+
 static int upload_local_table(fyg_plan* pl, int R, int cb, const void** dptr) {
     auto buf = std::make_unique<DevBuf>();
-    int rc;
-    if (cb == 8) {
-        std::vector<float2> h(R);
-        for (int t = 0; t < R; ++t) {
-            long double c, s;
-            twiddle_ld(t, R, &c, &s);
-            h[t] = make_float2((float)c, (float)s);
-        }
-        rc = buf->upload(h.data(), h.size() * sizeof(float2));
-    } else {
-        std::vector<double2> h(R);
-        for (int t = 0; t < R; ++t) {
-            long double c, s;
-            twiddle_ld(t, R, &c, &s);
-            h[t] = make_double2((double)c, (double)s);
-        }
-        rc = buf->upload(h.data(), h.size() * sizeof(double2));
-    }
+    const std::vector<unsigned char> h = host_local_table(R, cb);
+    const int rc = buf->upload(h.data(), h.size());
     if (rc) return rc;
     *dptr = buf->ptr;
     pl->tables.push_back(std::move(buf));
     return FYG_OK;
 }
 
-// two-level table of w_L: hi[i] = w^(i 2^s), lo[j] = w^j; float tables hold (hi, lo) pairs
 static int upload_two_level(fyg_plan* pl, uint64_t L, int cb, const void** hi, const void** lo, int* shift) {
-    int s = 0;
-    while ((1ull << (2 * s)) < L) ++s;  // 2^s ~ sqrt(L)
-    if (s < 1) s = 1;
-    const uint64_t B = 1ull << s, nhi = (L + B - 1) / B;
+    std::vector<unsigned char> th, tl;
+    host_two_level(L, cb, th, tl, shift);
     auto bh = std::make_unique<DevBuf>(), bl = std::make_unique<DevBuf>();
-    int rc;
-    if (cb == 8) {
-        auto pack = [](long double c, long double sn) {
-            const float ch = (float)c, sh = (float)sn;
-            return make_float4(ch, sh, (float)(c - (long double)ch), (float)(sn - (long double)sh));
-        };
-        std::vector<float4> th(nhi), tl(B);
-        for (uint64_t i = 0; i < nhi; ++i) { long double c, sn; twiddle_ld(i * B, L, &c, &sn); th[i] = pack(c, sn); }
-        for (uint64_t j = 0; j < B; ++j) { long double c, sn; twiddle_ld(j, L, &c, &sn); tl[j] = pack(c, sn); }
-        rc = bh->upload(th.data(), th.size() * sizeof(float4));
-        if (!rc) rc = bl->upload(tl.data(), tl.size() * sizeof(float4));
-    } else {
-        std::vector<double2> th(nhi), tl(B);
-        for (uint64_t i = 0; i < nhi; ++i) { long double c, sn; twiddle_ld(i * B, L, &c, &sn); th[i] = make_double2((double)c, (double)sn); }
-        for (uint64_t j = 0; j < B; ++j) { long double c, sn; twiddle_ld(j, L, &c, &sn); tl[j] = make_double2((double)c, (double)sn); }
-        rc = bh->upload(th.data(), th.size() * sizeof(double2));
-        if (!rc) rc = bl->upload(tl.data(), tl.size() * sizeof(double2));
-    }
+    int rc = bh->upload(th.data(), th.size());
+    if (!rc) rc = bl->upload(tl.data(), tl.size());
     if (rc) return rc;
     *hi = bh->ptr;
     *lo = bl->ptr;
-    *shift = s;
     pl->tables.push_back(std::move(bh));
     pl->tables.push_back(std::move(bl));
     return FYG_OK;
@@ -399,7 +399,7 @@ struct PipeSpec {
     int C;                    // columns per tile (single-pass: transforms per CTA)
 };
 
-static int pick_variant(int compute_cb, int tin_cb, int tout_cb, int cls) {
+int pick_variant(int compute_cb, int tin_cb, int tout_cb, int cls) {
     if (compute_cb == 8) return cls <= 16 ? KV_F32_C16 : KV_F32_C32;
     if (tin_cb == 16 && tout_cb == 16) return KV_F64_C16;
     if (tin_cb == 8 && tout_cb == 16) return KV_F64_IF32_C16;
@@ -408,7 +408,7 @@ static int pick_variant(int compute_cb, int tin_cb, int tout_cb, int cls) {
 }
 
 // about 16 elements per thread
-static int threads_for(int R, int C, int maxt) {
+int threads_for(int R, int C, int maxt) {
     int t = (R * C + 15) / 16;
     t = (t + 31) / 32 * 32;
     t = std::max(t, 64);

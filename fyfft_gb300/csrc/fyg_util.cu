@@ -37,6 +37,11 @@ bool g_dev_init[128] = {};
 
 }  // namespace
 
+void codelet_consts(CodeletConsts<float>* kf, CodeletConsts<double>* kd) {
+    fill_consts(*kf);
+    fill_consts(*kd);
+}
+
 cudaError_t ensure_device_constants() {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

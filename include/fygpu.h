@@ -116,6 +116,19 @@ int fyg_batch_execute(fyg_batch* batch, const void* in, void* out, const int64_t
 int fyg_batch_execute_plain(fyg_batch* batch, const void* in, void* out, int direction,
                             void* stream);
 
+/* Allocation-free transform: no counterpart in the reference.  For callers that cannot call
+ * cudaMalloc (code running during CUDA graph capture, host applications that own all device
+ * memory and pass a plugin only its buffers, latency-bound loops that cannot take the
+ * synchronization an allocation may cause).  Runs `batch` contiguous transforms of a 13-smooth
+ * length n with the multi-pass kernel; its scratch and twiddle tables live in a fixed 20 MiB
+ * file-scope device array (held by every GPU that loads the library until exit).  Limit:
+ * n * batch * element size <= 16 MiB (half that when n needs three or more passes); larger
+ * sizes return FYG_ERR_INVALID_LENGTH.  in/out must be device pointers; nothing is allocated.
+ * The first call on a device resolves the array's address and uploads constants, so make it
+ * before any stream capture.  All calls share the array: calls that overlap on the GPU race. */
+int fyg_execute_noalloc(size_t n, size_t batch, int dtype, int direction, const void* in, void* out,
+                        void* stream);
+
 /* Last error on the calling thread ("" if none). */
 const char* fyg_last_error_string(void);
 
