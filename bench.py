@@ -258,9 +258,46 @@ def run_ours(args, rank: int, world: int):
         "clocks": clk,
         "per_size": per_size,
     }
+    if not args.no_uneven:
+        out["batched_vs_plain"] = uneven_batch(dev, stream)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(items, args, check=(plans, yout))
     return out
+
+
+def uneven_batch(dev: int, stream, reps: int = 10):
+    """The mixed-length batch (4096 lengths in [16, 65536], 7-smooth / prime / other, seed 2):
+    one persistent launch (CUDA graph) against one launch sequence per transform."""
+    import torch
+    import fyfft_gb300 as fg
+    from fyfft_gb300.workloads import uneven_lengths
+    lengths = uneven_lengths(4096, 2)
+    t0 = time.perf_counter()
+    b = fg.UnevenBatch(lengths)
+    create_s = time.perf_counter() - t0
+    x = torch.from_numpy(fg.fill_random(2, sum(lengths), np.complex64, "uniform")).to(f"cuda:{dev}")
+    y = torch.empty_like(x)
+    fl = sum(flops(n) for n in lengths)
+    res = {"workload": "4096 complex<float> transforms, lengths log-uniform in [16, 65536] "
+                       "(0.70 7-smooth / 0.15 prime / 0.15 other), uniform[-1,1] seed 2, packed back to back",
+           "points": int(sum(lengths)), "distinct_lengths": len(set(lengths)), "create_s": round(create_s, 2)}
+    for name, f in (("batched", lambda: b.execute(x, y, stream=stream)),
+                    ("plain", lambda: b.execute_plain(x, y, stream=stream))):
+        for _ in range(3):
+            f()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            f()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        res[f"{name}_ms"] = round(ms, 4)
+        res[f"{name}_gflops"] = round(fl / (ms * 1e-3) / 1e9, 1)
+    res["status"] = b.status(stream)
+    res["speedup"] = round(res["plain_ms"] / res["batched_ms"], 2)
+    return res
 
 
 def read_traffic(n: int, pass_index: int):
@@ -362,6 +399,7 @@ def main():
     ap.add_argument("--workload", default="sweep", choices=["sweep", "c1", "c5"])
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the mixed-length batch comparison")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 

@@ -35,7 +35,8 @@ EXPORTED_SYMBOLS = (
     "fyg_plan_create", "fyg_plan_destroy", "fyg_execute", "fyg_execute_adjoint", "fyg_strategy",
     "fyg_gpu_strategy", "fyg_plan_info", "fyg_plan_launches", "fyg_plan_profile",
     "fyg_plan_profile_read", "fyg_batch_create", "fyg_batch_destroy",
-    "fyg_batch_execute", "fyg_batch_execute_plain", "fyg_execute_noalloc", "fyg_last_error_string",
+    "fyg_batch_execute", "fyg_batch_execute_plain", "fyg_batch_status", "fyg_batch_inject_stall",
+    "fyg_execute_noalloc", "fyg_last_error_string",
     "fyg_fill_random",
     "fyg_fill_random_device", "fyg_version",
 )
@@ -82,6 +83,8 @@ def lib() -> ctypes.CDLL:
         L.fyg_batch_destroy.argtypes = [vp]
         L.fyg_batch_execute.argtypes = [vp, vp, vp, vp, i, vp]
         L.fyg_batch_execute_plain.argtypes = [vp, vp, vp, i, vp]
+        L.fyg_batch_status.argtypes = [vp, vp]
+        L.fyg_batch_inject_stall.argtypes = [vp, i, i]
         L.fyg_execute_noalloc.argtypes = [sz, sz, i, i, vp, vp, vp]
         L.fyg_last_error_string.restype = ctypes.c_char_p
         L.fyg_fill_random.argtypes = [u64, i, i, sz, vp]
@@ -265,9 +268,19 @@ class UnevenBatch:
     def execute(self, x, y, invert: bool = False, offsets_dev=None, stream=None) -> None:
         px, _, _, _ = _buffer_ptr(x)
         py, _, _, _ = _buffer_ptr(y)
-        po = None if offsets_dev is None else _buffer_ptr(offsets_dev)[0]
+        po = None
+        if offsets_dev is not None:
+            po = offsets_dev.data_ptr() if hasattr(offsets_dev, "data_ptr") else int(offsets_dev)
         check(lib().fyg_batch_execute(self._h, px, py, po, FYG_INVERSE if invert else FYG_FORWARD,
                                       _stream_handle(stream)))
+
+    def status(self, stream=None) -> int:
+        """Synchronizes and returns the device status of the last execute (0 = OK)."""
+        return lib().fyg_batch_status(self._h, _stream_handle(stream))
+
+    def inject_stall(self, enable: bool = True, timeout_ms: int = 200) -> None:
+        """Test hook: make a pass dependency unreachable so the next execute times out."""
+        check(lib().fyg_batch_inject_stall(self._h, int(enable), timeout_ms))
 
     def execute_plain(self, x, y, invert: bool = False, stream=None) -> None:
         px, _, _, _ = _buffer_ptr(x)

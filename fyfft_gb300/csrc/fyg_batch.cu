@@ -1,24 +1,279 @@
-// fyg_batch.cu -- uneven-length batches (many transforms of different lengths, packed back to
-// back).  No counterpart in the reference, which runs one transform per dispatch call.
+// fyg_batch.cu -- uneven-length batches: many transforms of different lengths, packed back to
+// back, run by one persistent kernel over a device work queue and launched as a CUDA graph.
+// No counterpart in the reference, which runs one transform per dispatch call.
+//
+// Work decomposition: transforms of equal length form a group served by one plan (batch =
+// multiplicity) whose user-buffer passes address the packed buffers through an offsets table.
+// Every pass of every group is a descriptor (its PassParams); a work item is one tile of one
+// descriptor.  Items are queued phase by phase (all first passes, then all second passes, ...),
+// longest groups first within a phase.  A CTA pops items in order with an atomic counter; an
+// item of pass p+1 waits until all tiles of pass p of its group are done.  Because items are
+// popped in queue order and every popped item is held by a running CTA, the item it waits for
+// is already being processed: the wait always ends.  It is still bounded (1 s by default): on
+// expiry the kernel sets an error word and an abort flag, every CTA returns, and
+// fyg_batch_status reports FYG_ERR_TIMEOUT.
 #include <algorithm>
 #include <map>
 #include <memory>
+#include <mutex>
+#include <numeric>
 #include <vector>
 
 #include "fyg_host.h"
+#include "fyg_k_variant.cuh"
+
+namespace fyg {
+
+constexpr int kBatchThreads = 256;
+constexpr int kBatchErrTimeout = 2;
+
+struct BatchArgs {
+    const PassParams* descs;
+    const int2* items;
+    int n_items;
+    const int* need;         // tiles per descriptor
+    const int* dep;          // descriptor each descriptor waits for (-1: none)
+    int* done;               // completed tiles per descriptor
+    int* head;               // queue head
+    int* err;
+    int* abort_flag;
+    const void* user_in;
+    void* user_out;
+    const int64_t* offsets;  // element offset of every transform in the packed buffers
+    unsigned long long timeout_ns;
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+template <int CLASS>
+__global__ void __launch_bounds__(kBatchThreads) k_batch(const __grid_constant__ BatchArgs a) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    PassParams* sp = reinterpret_cast<PassParams*>(smraw);
+    unsigned char* tsm = smraw + ((sizeof(PassParams) + 15) & ~(size_t)15);
+    __shared__ int s_item, s_ok;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            int it = *reinterpret_cast<volatile int*>(a.abort_flag) ? a.n_items : atomicAdd(a.head, 1);
+            if (it > a.n_items) it = a.n_items;
+            int ok = 1;
+            if (it < a.n_items) {
+                const int dep = a.dep[a.items[it].x];
+                if (dep >= 0) {
+                    const int need = a.need[dep];
+                    const unsigned long long t0 = global_ns();
+                    while (atomicAdd(&a.done[dep], 0) < need) {
+                        if (*reinterpret_cast<volatile int*>(a.abort_flag)) { ok = 0; break; }
+                        if (global_ns() - t0 > a.timeout_ns) {
+                            atomicOr(a.err, kBatchErrTimeout);
+                            atomicExch(a.abort_flag, 1);
+                            ok = 0;
+                            break;
+                        }
+                        __nanosleep(200);
+                    }
+                    __threadfence();
+                }
+            }
+            s_item = it;
+            s_ok = ok;
+        }
+        __syncthreads();
+        const int it = s_item;
+        if (it >= a.n_items) break;
+        if (s_ok) {
+            const int2 d = a.items[it];
+            const int4* src = reinterpret_cast<const int4*>(a.descs + d.x);
+            int4* dst = reinterpret_cast<int4*>(sp);
+            for (int w = threadIdx.x; w < (int)(sizeof(PassParams) / 16); w += blockDim.x) dst[w] = src[w];
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                if (sp->in_user) { sp->in = a.user_in; sp->in_offsets = a.offsets; }
+                if (sp->out_user) { sp->out = a.user_out; sp->out_offsets = a.offsets; }
+            }
+            __syncthreads();
+            if (sp->g.colmajor) tile_body<float, float, float, CLASS, true>(*sp, d.y, tsm);
+            else tile_body<float, float, float, CLASS, false>(*sp, d.y, tsm);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                __threadfence();
+                atomicAdd(&a.done[d.x], 1);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int CLASS>
+static cudaError_t launch_batch(const BatchArgs& a, size_t smem, cudaStream_t st, int* grid_out) {
+    auto kern = k_batch<CLASS>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBatchThreads, smem);
+    if (e != cudaSuccess) return e;
+    int grid = std::max(1, sms * std::max(per_sm, 1));
+    grid = std::min(grid, std::max(a.n_items, 1));
+    *grid_out = grid;
+    kern<<<grid, kBatchThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace fyg
+
+using namespace fyg;
 
 struct fyg_batch {
     std::vector<size_t> lengths;
-    std::vector<int64_t> offsets;     // packed offsets (elements)
+    std::vector<int64_t> offsets;              // packed offsets (elements)
     int dtype = FYG_C32;
     int flags = 0;
-    std::map<size_t, fyg_plan*> plans; // one batch-1 plan per distinct length
+    std::map<size_t, fyg_plan*> group_plans;   // per distinct length: batch = multiplicity
+    std::map<size_t, std::vector<int>> members;
+    std::map<size_t, fyg_plan*> single_plans;  // per distinct length: batch 1 (plain path)
+    // persistent execution state (FP32 batches)
+    bool persistent = false;
+    int cls = 16;
+    size_t smem = 0;
+    int n_descs = 0, n_items = 0;
+    DevBuf d_descs_fwd, d_descs_inv, d_items, d_need, d_dep, d_ids, d_offsets, d_state;
+    std::vector<int> need_host;
+    unsigned long long timeout_ns = 1000000000ull;
+    // one instantiated graph per (direction, in, out, offsets)
+    struct GraphKey {
+        int dir; const void* in; void* out; const int64_t* off;
+        bool operator<(const GraphKey& o) const {
+            return std::tie(dir, in, out, off) < std::tie(o.dir, o.in, o.out, o.off);
+        }
+    };
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+    cudaStream_t cap_stream = nullptr;
+    int last_grid = 0;
+
+    int* done_ptr() { return reinterpret_cast<int*>(d_state.ptr); }
+    int* head_ptr() { return done_ptr() + n_descs; }
+    int* err_ptr() { return head_ptr() + 1; }
+    int* abort_ptr() { return head_ptr() + 2; }
+
     ~fyg_batch() {
-        for (auto& kv : plans) fyg_plan_destroy(kv.second);
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+        if (cap_stream) cudaStreamDestroy(cap_stream);
+        for (auto& kv : group_plans) fyg_plan_destroy(kv.second);
+        for (auto& kv : single_plans) fyg_plan_destroy(kv.second);
     }
 };
 
-using namespace fyg;
+namespace {
+
+// Builds the descriptor tables and the work queue for one direction set (forward and inverse
+// share items, need and dep; only the PassParams differ).
+int build_persistent(fyg_batch* b) {
+    std::vector<PassParams> fwd, inv;
+    std::vector<int> need, dep, ids, fwd_id0, inv_id0;
+    struct G { size_t len; int first_desc; int npass; double work; };
+    std::vector<G> groups;
+    size_t smem = 0;
+    int cls = 16;
+    for (auto& kv : b->group_plans) {
+        const size_t len = kv.first;
+        fyg_plan* pl = kv.second;
+        if (pl->strategy == GS_COPY || pl->chunk != pl->batch || pl->compute_bytes != 8) return FYG_ERR_UNSUPPORTED;
+        const std::vector<int>& mem = b->members[len];
+        const int id0 = (int)ids.size();
+        ids.insert(ids.end(), mem.begin(), mem.end());
+        G g{len, (int)fwd.size(), (int)pl->fwd.size(), (double)len * mem.size()};
+        for (int dirn = 0; dirn < 2; ++dirn) {
+            const std::vector<PassDesc>& pipe = dirn == 0 ? pl->fwd : pl->inv;
+            for (size_t i = 0; i < pipe.size(); ++i) {
+                const PassDesc& d = pipe[i];
+                PassParams p = d.p;
+                p.ncols = (int64_t)pl->batch * p.Rr;
+                p.x0buf = pl->x0buf.ptr;
+                p.dcbuf = pl->dcbuf.ptr;
+                p.in_user = d.in_role == ROLE_IN;
+                p.out_user = d.out_role == ROLE_OUT;
+                p.in = d.in_role == ROLE_S0 ? pl->scratch0.ptr : d.in_role == ROLE_S1 ? pl->scratch1.ptr : nullptr;
+                p.out = d.out_role == ROLE_S0 ? pl->scratch0.ptr : d.out_role == ROLE_S1 ? pl->scratch1.ptr : nullptr;
+                p.in_offsets = p.out_offsets = nullptr;
+                p.ids = nullptr;   // set once the id table is on the device
+                if (dirn == 0) {
+                    fwd.push_back(p);
+                    fwd_id0.push_back(id0);
+                    need.push_back((int)((p.ncols + p.g.C - 1) / p.g.C));
+                    dep.push_back(i == 0 ? -1 : (int)fwd.size() - 2);
+                    smem = std::max(smem, d.smem);
+                    if (d.kv == KV_F32_C32) cls = 32;
+                } else {
+                    inv.push_back(p);
+                    inv_id0.push_back(id0);
+                }
+            }
+        }
+        groups.push_back(g);
+    }
+    int rc = b->d_ids.upload(ids.data(), std::max<size_t>(ids.size(), 1) * sizeof(int));
+    if (rc) return rc;
+    for (size_t i = 0; i < fwd.size(); ++i) fwd[i].ids = reinterpret_cast<const int*>(b->d_ids.ptr) + fwd_id0[i];
+    for (size_t i = 0; i < inv.size(); ++i) inv[i].ids = reinterpret_cast<const int*>(b->d_ids.ptr) + inv_id0[i];
+    // queue: phase by phase, longest groups first
+    std::vector<int> order(groups.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](int x, int y) { return groups[x].work > groups[y].work; });
+    int maxp = 0;
+    for (auto& g : groups) maxp = std::max(maxp, g.npass);
+    std::vector<int2> items;
+    for (int ph = 0; ph < maxp; ++ph)
+        for (int gi : order) {
+            const G& g = groups[gi];
+            if (ph >= g.npass) continue;
+            const int desc = g.first_desc + ph;
+            for (int t = 0; t < need[desc]; ++t) items.push_back(make_int2(desc, t));
+        }
+    b->n_descs = (int)fwd.size();
+    b->n_items = (int)items.size();
+    b->need_host = need;
+    b->smem = ((sizeof(PassParams) + 15) & ~(size_t)15) + smem;
+    b->cls = cls;
+    if (b->smem > 232448) return set_error(FYG_ERR_UNSUPPORTED, "batch tile exceeds shared memory");
+    rc = b->d_descs_fwd.upload(fwd.data(), fwd.size() * sizeof(PassParams));
+    if (!rc) rc = b->d_descs_inv.upload(inv.data(), inv.size() * sizeof(PassParams));
+    if (!rc) rc = b->d_items.upload(items.data(), std::max<size_t>(items.size(), 1) * sizeof(int2));
+    if (!rc) rc = b->d_need.upload(need.data(), need.size() * sizeof(int));
+    if (!rc) rc = b->d_dep.upload(dep.data(), dep.size() * sizeof(int));
+    if (!rc) rc = b->d_offsets.upload(b->offsets.data(), b->offsets.size() * sizeof(int64_t));
+    if (!rc) rc = b->d_state.alloc((b->n_descs + 4) * sizeof(int));
+    return rc;
+}
+
+int launch_persistent(fyg_batch* b, const void* in, void* out, const int64_t* offs, int direction,
+                      cudaStream_t st) {
+    BatchArgs a;
+    a.descs = reinterpret_cast<const PassParams*>(direction == FYG_INVERSE ? b->d_descs_inv.ptr : b->d_descs_fwd.ptr);
+    a.items = reinterpret_cast<const int2*>(b->d_items.ptr);
+    a.n_items = b->n_items;
+    a.need = reinterpret_cast<const int*>(b->d_need.ptr);
+    a.dep = reinterpret_cast<const int*>(b->d_dep.ptr);
+    a.done = b->done_ptr();
+    a.head = b->head_ptr();
+    a.err = b->err_ptr();
+    a.abort_flag = b->abort_ptr();
+    a.user_in = in;
+    a.user_out = out;
+    a.offsets = offs ? offs : reinterpret_cast<const int64_t*>(b->d_offsets.ptr);
+    a.timeout_ns = b->timeout_ns;
+    cudaError_t e = cudaMemsetAsync(b->d_state.ptr, 0, (b->n_descs + 4) * sizeof(int), st);
+    if (e != cudaSuccess) return cuda_error(e, "batch state reset");
+    e = b->cls > 16 ? launch_batch<32>(a, b->smem, st, &b->last_grid) : launch_batch<16>(a, b->smem, st, &b->last_grid);
+    if (e != cudaSuccess) return cuda_error(e, "persistent batch launch");
+    return FYG_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -35,13 +290,24 @@ int fyg_batch_create(const size_t* lengths, size_t count, int dtype, int flags, 
         if (lengths[i] < 1) return set_error(FYG_ERR_INVALID_LENGTH, "length must be >= 1");
         b->lengths.push_back(lengths[i]);
         b->offsets.push_back(off);
+        b->members[lengths[i]].push_back((int)i);
         off += (int64_t)lengths[i];
-        if (!b->plans.count(lengths[i])) {
-            fyg_plan* p = nullptr;
-            int rc = fyg_plan_create(lengths[i], dtype, 1, flags, &p);
-            if (rc) return rc;
-            b->plans[lengths[i]] = p;
-        }
+    }
+    for (auto& kv : b->members) {
+        fyg_plan* p = nullptr;
+        int rc = fyg_plan_create(kv.first, dtype, kv.second.size(),
+                                 flags | FYG_FLAG_NO_L2_CHUNK | FYG_FLAG_SMALL_TILES, &p);
+        if (rc) return rc;
+        b->group_plans[kv.first] = p;
+        rc = fyg_plan_create(kv.first, dtype, 1, flags, &p);
+        if (rc) return rc;
+        b->single_plans[kv.first] = p;
+    }
+    if (dtype == FYG_C32 && count > 0) {
+        int rc = build_persistent(b.get());
+        if (rc == FYG_OK) b->persistent = true;
+        else if (rc != FYG_ERR_UNSUPPORTED) return rc;
+        clear_error();
     }
     *out = b.release();
     return FYG_OK;
@@ -59,7 +325,7 @@ int fyg_batch_execute_plain(fyg_batch* b, const void* in, void* out, int directi
     for (size_t i = 0; i < b->lengths.size(); ++i) {
         const char* x = (const char*)in + b->offsets[i] * eb;
         char* y = (char*)out + b->offsets[i] * eb;
-        int rc = fyg_execute(b->plans[b->lengths[i]], x, y, direction, stream);
+        int rc = fyg_execute(b->single_plans[b->lengths[i]], x, y, direction, stream);
         if (rc) return rc;
     }
     return FYG_OK;
@@ -67,8 +333,77 @@ int fyg_batch_execute_plain(fyg_batch* b, const void* in, void* out, int directi
 
 int fyg_batch_execute(fyg_batch* b, const void* in, void* out, const int64_t* offsets_dev, int direction,
                       void* stream) {
-    (void)offsets_dev;
-    return fyg_batch_execute_plain(b, in, out, direction, stream);
+    clear_error();
+    if (!b || !in || !out) return set_error(FYG_ERR_NULL_PTR, "null argument");
+    if (direction != FYG_FORWARD && direction != FYG_INVERSE)
+        return set_error(FYG_ERR_INVALID_ARG, "direction must be FYG_FORWARD or FYG_INVERSE");
+    if (b->lengths.empty()) return FYG_OK;
+    const cudaStream_t st = (cudaStream_t)stream;
+    if (!b->persistent) {
+        // FP64 batches: one launch sequence per group of equal lengths
+        if (offsets_dev) return set_error(FYG_ERR_UNSUPPORTED, "custom offsets need an FP32 batch");
+        return fyg_batch_execute_plain(b, in, out, direction, stream);
+    }
+    fyg_batch::GraphKey key{direction, in, out, offsets_dev};
+    auto it = b->graphs.find(key);
+    if (it == b->graphs.end()) {
+        if (!b->cap_stream) {
+            cudaError_t e = cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking);
+            if (e != cudaSuccess) return cuda_error(e, "capture stream");
+        }
+        cudaError_t e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_error(e, "begin capture");
+        int rc = launch_persistent(b, in, out, offsets_dev, direction, b->cap_stream);
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(b->cap_stream, &g);
+        if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+        if (e != cudaSuccess) return cuda_error(e, "end capture");
+        cudaGraphExec_t ex = nullptr;
+        e = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_error(e, "graph instantiate");
+        it = b->graphs.emplace(key, ex).first;
+    }
+    cudaError_t e = cudaGraphLaunch(it->second, st);
+    if (e != cudaSuccess) return cuda_error(e, "graph launch");
+    return FYG_OK;
+}
+
+int fyg_batch_status(fyg_batch* b, void* stream) {
+    clear_error();
+    if (!b) return set_error(FYG_ERR_NULL_PTR, "null batch");
+    if (!b->persistent) return FYG_OK;
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_error(e, "stream synchronize");
+    int err = 0;
+    e = cudaMemcpy(&err, b->err_ptr(), sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_error(e, "status read");
+    if (err & kBatchErrTimeout)
+        return set_error(FYG_ERR_TIMEOUT, "a work item waited longer than the batch's limit for its dependency");
+    return FYG_OK;
+}
+
+int fyg_batch_inject_stall(fyg_batch* b, int enable, int timeout_ms) {
+    clear_error();
+    if (!b) return set_error(FYG_ERR_NULL_PTR, "null batch");
+    if (!b->persistent) return set_error(FYG_ERR_UNSUPPORTED, "batch has no persistent path");
+    std::vector<int> need = b->need_host;
+    if (enable) {
+        // the first descriptor another one waits for: its completion count becomes unreachable
+        std::vector<int> dep(b->n_descs);
+        cudaError_t e = cudaMemcpy(dep.data(), b->d_dep.ptr, dep.size() * sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_error(e, "dep read");
+        int victim = -1;
+        for (int d : dep) if (d >= 0) { victim = d; break; }
+        if (victim < 0) return set_error(FYG_ERR_UNSUPPORTED, "no multi-pass group to stall");
+        need[victim] = 1 << 30;
+    }
+    b->timeout_ns = enable ? (unsigned long long)std::max(timeout_ms, 1) * 1000000ull : 1000000000ull;
+    for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    b->graphs.clear();
+    cudaError_t e = cudaMemcpy(b->d_need.ptr, need.data(), need.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_error(e, "need upload");
+    return FYG_OK;
 }
 
 }  // extern "C"

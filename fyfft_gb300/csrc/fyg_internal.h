@@ -32,6 +32,12 @@ cudaError_t ensure_device_constants();
 // Host values of the codelet constant tables (for translation units that upload their own).
 void codelet_consts(CodeletConsts<float>* kf, CodeletConsts<double>* kd);
 
+// Every translation unit that launches kernels holds its own __constant__ codelet tables (no
+// relocatable device code) and registers an uploader for them at static initialization;
+// ensure_device_constants() runs all registered uploaders once per device.
+using ConstUploader = cudaError_t (*)(const CodeletConsts<float>&, const CodeletConsts<double>&);
+bool register_const_uploader(ConstUploader f);
+
 // Device RNG fill (fyg_fill_random_device).
 cudaError_t launch_fill_random(uint64_t seed, int dist, int dtype, size_t n, void* out,
                                cudaStream_t st);

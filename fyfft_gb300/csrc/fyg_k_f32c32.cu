@@ -4,7 +4,4 @@ namespace fyg {
 cudaError_t launch_f32c32(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st) {
     return launch_variant<float, float, float, 32>(p, grid, threads, smem, st);
 }
-cudaError_t upload_consts_f32c32(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd) {
-    return upload_consts_tu(kf, kd);
-}
 }  // namespace fyg

@@ -7,7 +7,4 @@ cudaError_t launch_mixed(int kv, const PassParams& p, unsigned grid, int threads
     if (kv == KV_F64_OF32_C16) return launch_variant<double, double, float, 16>(p, grid, threads, smem, st);
     return launch_variant<double, float, float, 16>(p, grid, threads, smem, st);
 }
-cudaError_t upload_consts_mixed(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd) {
-    return upload_consts_tu(kf, kd);
-}
 }  // namespace fyg

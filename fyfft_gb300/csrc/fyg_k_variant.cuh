@@ -28,10 +28,11 @@ cudaError_t launch_variant(const PassParams& p, unsigned grid, int threads, size
 }
 
 // Copies the codelet constants into this translation unit's __constant__ tables.
-inline cudaError_t upload_consts_tu(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd) {
+static cudaError_t upload_consts_tu(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd) {
     cudaError_t e = cudaMemcpyToSymbol(g_kf, &kf, sizeof(kf));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_kd, &kd, sizeof(kd));
     return e;
 }
+static const bool g_consts_registered = register_const_uploader(&upload_consts_tu);
 
 }  // namespace fyg

@@ -122,8 +122,8 @@ __device__ __forceinline__ Col<T> colmajor_col(const PassParams& p, int64_t q) {
     ci.jj = 0;
     ci.k = 0;
     ci.out_j = 0;
-    ci.in_base = q * p.idist;
-    ci.out_base = q * p.odist;
+    ci.in_base = ci.valid ? transform_base(p.in_offsets, p.ids, q, p.idist) : 0;
+    ci.out_base = ci.valid ? transform_base(p.out_offsets, p.ids, q, p.odist) : 0;
     ci.x0 = mk<cplx<T>>(T(0), T(0));
     return ci;
 }
@@ -171,7 +171,7 @@ __device__ __forceinline__ void load_general(const PassParams& p, cplx<T>* buf, 
                 if (ci.valid) {
                     const int gidx = ci.jj + n * Rr;
                     if constexpr (MODE == LD_PLAIN || MODE == LD_PLAIN_TW) {
-                        v = to_c(gin[ci.in_base + gidx], T());
+                        v = to_c(ld_data(gin + ci.in_base + gidx), T());
                         if (conj_in) v = cconj(v);
                         if constexpr (MODE == LD_PLAIN_TW) {
                             if (ci.k != 0 && n != 0)
@@ -179,14 +179,14 @@ __device__ __forceinline__ void load_general(const PassParams& p, cplx<T>* buf, 
                         }
                     } else if constexpr (MODE == LD_CHIRP) {
                         if (gidx < nvalid) {
-                            v = to_c(gin[ci.in_base + gidx], T());
+                            v = to_c(ld_data(gin + ci.in_base + gidx), T());
                             if (conj_in) v = cconj(v);
                             v = cmul(v, cconj(__ldg(chirp + gidx)));
                         }
                     } else {
                         const int t = __ldg(gather + gidx);
                         if (t >= 0) {
-                            v = to_c(gin[ci.in_base + t], T());
+                            v = to_c(ld_data(gin + ci.in_base + t), T());
                             if (conj_in) v = cconj(v);
                         }
                     }
@@ -220,7 +220,7 @@ __device__ __forceinline__ void load_elem_plain(const PassParams& p, cplx<T>* bu
         for (int i = 0; i < UNR; ++i) {
             const int n = n0 + i * G;
             u[i] = mk<T2>(T(0), T(0));
-            if (n < R && mc.valid) u[i] = to_c(src[(int64_t)n * Rr], T());
+            if (n < R && mc.valid) u[i] = to_c(ld_data(src + (int64_t)n * Rr), T());
         }
 #pragma unroll
         for (int i = 0; i < UNR; ++i) {
@@ -255,7 +255,7 @@ __device__ __forceinline__ void load_flat_plain(const PassParams& p, cplx<T>* bu
         for (int i = 0; i < UNR; ++i) {
             const int e = e0 + i * nthr;
             u[i] = mk<T2>(T(0), T(0));
-            if (e < Ev) u[i] = to_c(src[e], T());
+            if (e < Ev) u[i] = to_c(ld_data(src + e), T());
         }
 #pragma unroll
         for (int i = 0; i < UNR; ++i) {
@@ -383,10 +383,9 @@ __device__ __forceinline__ void store_flat_plain(const PassParams& p, const cplx
 // ------------------------------------------------------------------------------------------
 // The kernel
 // ------------------------------------------------------------------------------------------
-// TAG only distinguishes instantiations made by different translation units.
-template <typename T, typename TI, typename TO, int CLASS, bool COLMAJOR, int TAG = 0>
-__global__ void __launch_bounds__(kMaxThreads) k_pass(const __grid_constant__ PassParams p) {
-    extern __shared__ __align__(16) unsigned char smraw[];
+// One tile (tile index `tile` of the pass described by p) with the CTA's threads.
+template <typename T, typename TI, typename TO, int CLASS, bool COLMAJOR>
+__device__ __forceinline__ void tile_body(const PassParams& p, int64_t tile, unsigned char* smraw) {
     using T2 = cplx<T>;
     using IN2 = cplx<TI>;
     const int R = p.g.R, C = p.g.C;
@@ -399,15 +398,15 @@ __global__ void __launch_bounds__(kMaxThreads) k_pass(const __grid_constant__ Pa
     L.C = C;
     L.lc = p.g.log2C;
     L.pitch = COLMAJOR ? colmajor_pitch(R) : C + 1;
-    const int64_t q0 = (int64_t)blockIdx.x * C;
+    const int64_t q0 = tile * C;
     const IN2* gin = reinterpret_cast<const IN2*>(p.in);
     const int E = R * C;
     const int nthr = blockDim.x;
     constexpr int UNR = sizeof(T) == 4 ? 16 : 8;
     const bool plain_in = p.load_mode == LD_PLAIN;
     const bool plain_out = p.store_mode == ST_PLAIN;
-    const bool flat_in = COLMAJOR && plain_in && p.idist == R;
-    const bool flat_out = COLMAJOR && plain_out && p.odist == R;
+    const bool flat_in = COLMAJOR && plain_in && p.idist == R && !p.in_offsets;
+    const bool flat_out = COLMAJOR && plain_out && p.odist == R && !p.out_offsets;
 
     // ---- stage schedule; per-column head for the general paths (output base, validity, x0) ----
     if (threadIdx.x < kMaxStages) {
@@ -425,7 +424,8 @@ __global__ void __launch_bounds__(kMaxThreads) k_pass(const __grid_constant__ Pa
             const Col<T> ci = COLMAJOR ? colmajor_col<T>(p, q0 + c) : make_col<T, TI>(p, q0 + c);
             T2 x0 = mk<T2>(T(0), T(0));
             if (ci.valid && (p.store_mode == ST_SCATTER || (p.x0_from_in && p.x0buf))) {
-                x0 = p.x0_from_in ? to_c(gin[ci.in_base], T()) : reinterpret_cast<const T2*>(p.x0buf)[ci.b];
+                x0 = p.x0_from_in ? to_c(ld_data(gin + ci.in_base), T())
+                                 : ld_data(reinterpret_cast<const T2*>(p.x0buf) + ci.b);
                 if (p.x0_from_in && p.x0buf && ci.jj == 0) reinterpret_cast<T2*>(p.x0buf)[ci.b] = x0;
             }
             ColHead<T> h;
@@ -503,6 +503,13 @@ __global__ void __launch_bounds__(kMaxThreads) k_pass(const __grid_constant__ Pa
         if (plain_out) store_elem_plain<T, TI, TO>(p, buf, L, q0);
         else store_general<T, TO, false>(p, buf, L, head);
     }
+}
+
+// TAG only distinguishes instantiations made by different translation units.
+template <typename T, typename TI, typename TO, int CLASS, bool COLMAJOR, int TAG = 0>
+__global__ void __launch_bounds__(kMaxThreads) k_pass(const __grid_constant__ PassParams p) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    tile_body<T, TI, TO, CLASS, COLMAJOR>(p, (int64_t)blockIdx.x, smraw);
 }
 
 }  // namespace fyg

@@ -54,7 +54,7 @@ struct TileGeom {
     FastDiv divR;              // R (element index -> column, column-major order)
 };
 
-struct PassParams {
+struct alignas(16) PassParams {
     TileGeom g;
     // transform-level geometry of this pass
     int64_t ncols;       // batch * Rr
@@ -85,7 +85,24 @@ struct PassParams {
     int mid;                 // fused spectrum multiply + second in-CTA FFT
     const void* spectrum;    // length L (T2)
     int* err;                // device error word (bounds violations are recorded, never trapped)
+    // uneven batches: transform b of this pass reads/writes the user buffers at
+    // offsets[ids[b]] (elements) instead of b * idist / b * odist; null for contiguous batches
+    const int64_t* in_offsets;
+    const int64_t* out_offsets;
+    const int* ids;
+    // uneven batches: 1 when in/out is the user buffer (patched in by the persistent kernel)
+    int in_user, out_user;
 };
+
+__device__ __forceinline__ int64_t transform_base(const int64_t* offs, const int* ids, int64_t b, int64_t dist) {
+    return offs ? offs[ids ? ids[b] : b] : b * dist;
+}
+
+// Data loads go through L2 only (ld.global.cg): every element is read once, and inside one
+// persistent batch launch a scratch region can be rewritten by a later pass, so no L1 copy of
+// it may survive.
+__device__ __forceinline__ float2 ld_data(const float2* p) { return __ldcg(p); }
+__device__ __forceinline__ double2 ld_data(const double2* p) { return __ldcg(p); }
 
 // Per-column state: the transform b a column belongs to, its column index jj inside the pass,
 // the inter-pass twiddle index k = jj mod Ns, the output column offset and the global bases.
@@ -155,8 +172,8 @@ __device__ __forceinline__ Col<T> make_col(const PassParams& p, int64_t q) {
     ci.k = (int)(jj - p.div_Ns.div(jj) * (uint32_t)p.Ns);
     const uint32_t qo = p.div_Ns_out.div(jj);
     ci.out_j = (int)(qo * (uint32_t)p.Ns_out * (uint32_t)p.g.R + (jj - qo * (uint32_t)p.Ns_out));
-    ci.in_base = (int64_t)b * p.idist;
-    ci.out_base = (int64_t)b * p.odist;
+    ci.in_base = transform_base(p.in_offsets, p.ids, b, p.idist);
+    ci.out_base = transform_base(p.out_offsets, p.ids, b, p.odist);
     ci.x0 = mk<T2>(T(0), T(0));
     return ci;
 }

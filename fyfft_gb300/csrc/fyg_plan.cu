@@ -184,19 +184,26 @@ static const int kRadices[] = {
     FYG_STAGE_RADICES(FYG_LIST)
 #undef FYG_LIST
 };
-static int max_radix(int cb) { return cb == 8 ? 32 : 16; }
+// Plans of uneven batches cap the stage radix at 16 so the persistent kernel compiles only the
+// smaller codelets (lower register pressure); set for the duration of such a plan's creation.
+static thread_local int t_radix_cap = 0;
+static int max_radix(int cb) {
+    const int r = cb == 8 ? 32 : 16;
+    return t_radix_cap ? std::min(r, t_radix_cap) : r;
+}
 
 // Radix schedule of an in-CTA transform of length R: fewest stages, then the smallest largest
 // radix (register pressure), then larger radices first.  Empty if R is not representable.
 std::vector<int> radices_for(int R, int cb) {
     static std::mutex mu;
     static std::map<std::pair<int, int>, std::vector<int>> memo;
+    const int rmax = max_radix(cb);
+    const int key = cb * 1000 + rmax;
     {
         std::lock_guard<std::mutex> lk(mu);
-        auto it = memo.find({R, cb});
+        auto it = memo.find({R, key});
         if (it != memo.end()) return it->second;
     }
-    const int rmax = max_radix(cb);
     // best[d] = (stages, largest radix) for every divisor d of R
     std::map<int, std::pair<int, int>> best;
     std::map<int, int> choice;
@@ -223,7 +230,7 @@ std::vector<int> radices_for(int R, int cb) {
         std::sort(out.begin(), out.end(), std::greater<int>());
     }
     std::lock_guard<std::mutex> lk(mu);
-    memo[{R, cb}] = out;
+    memo[{R, key}] = out;
     return out;
 }
 
@@ -526,7 +533,9 @@ static int make_plan(fyg_plan* pl) {
         return FYG_OK;
     }
     // ---- strategy ----
-    if (is_smooth(n, 13) && n <= 16384 && tile_fits(io_cb, (int)n, 1, true)) {
+    const size_t single_cap = (pl->flags & FYG_FLAG_SMALL_TILES) ? (100u << 10) : kSmemLimit;
+    if (is_smooth(n, 13) && n <= 16384 && tile_fits(io_cb, (int)n, 1, true) &&
+        smem_for(io_cb, (int)n, 1, true) <= single_cap) {
         ps.kind = GS_SINGLE;
         ps.L = n;
         ps.prad = {(int)n};
@@ -551,7 +560,8 @@ static int make_plan(fyg_plan* pl) {
     pl->compute_bytes = (pl->dtype == FYG_C64 || pl->conv_fp64) ? 16 : 8;
     const int cb = pl->compute_bytes;
     if (ps.kind != GS_SINGLE) {
-        if (conv && ps.L <= 16384 && tile_fits(cb, (int)ps.L, 1, true)) {
+        if (conv && ps.L <= 16384 && tile_fits(cb, (int)ps.L, 1, true) &&
+            smem_for(cb, (int)ps.L, 1, true) <= single_cap) {
             ps.prad = {(int)ps.L};
         } else if (!split_passes(ps.L, cb, conv, ps.prad)) {
             return set_error(FYG_ERR_UNSUPPORTED, "no pass decomposition for length " + std::to_string(ps.L));
@@ -856,7 +866,9 @@ int fyg_plan_create(size_t n, int dtype, size_t batch, int flags, fyg_plan** out
     pl->dtype = dtype;
     pl->flags = flags;
     pl->device = dev;
+    t_radix_cap = (flags & FYG_FLAG_SMALL_TILES) ? 16 : 0;
     int rc = make_plan(pl);
+    t_radix_cap = 0;
     if (rc) {
         delete pl;
         return rc;

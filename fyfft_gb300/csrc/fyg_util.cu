@@ -10,10 +10,14 @@
 
 namespace fyg {
 
-cudaError_t upload_consts_f32(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd);
-cudaError_t upload_consts_f64(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd);
-cudaError_t upload_consts_mixed(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd);
-cudaError_t upload_consts_f32c32(const CodeletConsts<float>& kf, const CodeletConsts<double>& kd);
+static std::vector<ConstUploader>& uploaders() {
+    static std::vector<ConstUploader> v;
+    return v;
+}
+bool register_const_uploader(ConstUploader f) {
+    uploaders().push_back(f);
+    return true;
+}
 
 namespace {
 
@@ -52,10 +56,11 @@ cudaError_t ensure_device_constants() {
     CodeletConsts<double> kd;
     fill_consts(kf);
     fill_consts(kd);
-    e = upload_consts_f32(kf, kd);
-    if (e == cudaSuccess) e = upload_consts_f64(kf, kd);
-    if (e == cudaSuccess) e = upload_consts_mixed(kf, kd);
-    if (e == cudaSuccess) e = upload_consts_f32c32(kf, kd);
+    e = cudaSuccess;
+    for (ConstUploader f : uploaders()) {
+        e = f(kf, kd);
+        if (e != cudaSuccess) break;
+    }
     if (e == cudaSuccess && dev < 128) g_dev_init[dev] = true;
     return e;
 }

@@ -54,6 +54,7 @@ extern "C" {
 #define FYG_FLAG_CONV_FP64 0x1   /* Rader/Bluestein convolution in FP64 even for FYG_C32 data */
 #define FYG_FLAG_CONV_FP32 0x2   /* force the FP32 convolution (disables the error-budget choice) */
 #define FYG_FLAG_NO_L2_CHUNK 0x4 /* process the whole batch per pass (no L2-resident chunking) */
+#define FYG_FLAG_SMALL_TILES 0x8 /* single-CTA transforms up to ~100 KB of shared memory, stage radix <= 16 */
 
 typedef struct fyg_plan fyg_plan;
 typedef struct fyg_batch fyg_batch;
@@ -111,6 +112,18 @@ int fyg_batch_destroy(fyg_batch* batch);
  * order given).  in/out device pointers. */
 int fyg_batch_execute(fyg_batch* batch, const void* in, void* out, const int64_t* offsets_dev,
                       int direction, void* stream);
+
+/* Waits for the batch's last fyg_batch_execute on `stream` and reports its device status:
+ * FYG_OK, or FYG_ERR_TIMEOUT when a work item waited longer than the batch's wait limit for
+ * the pass it depends on (the kernel then abandons the run and returns; the context stays
+ * usable). */
+int fyg_batch_status(fyg_batch* batch, void* stream);
+
+/* Test hook (host-side fault injection): with enable != 0, the completion count of the first
+ * pass another pass waits for becomes unreachable, so the next fyg_batch_execute gives up
+ * after `timeout_ms` and fyg_batch_status reports FYG_ERR_TIMEOUT; enable == 0 restores the
+ * batch.  No counterpart in the reference. */
+int fyg_batch_inject_stall(fyg_batch* batch, int enable, int timeout_ms);
 
 /* Same batch, one launch sequence per transform (the plain one-plan-per-launch path). */
 int fyg_batch_execute_plain(fyg_batch* batch, const void* in, void* out, int direction,

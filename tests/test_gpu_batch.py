@@ -1,0 +1,94 @@
+"""Uneven-length batch: one persistent launch over a device work queue (CUDA graph) against the
+FP64 oracle, the one-plan-per-launch path, custom offsets, and the bounded dependency wait."""
+import time
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import fyfft_gb300 as fg  # noqa: E402
+from fyfft_gb300.workloads import uneven_lengths  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def batch():
+    lengths = uneven_lengths(count=192, seed=2)
+    b = fg.UnevenBatch(lengths)
+    x = fg.fill_random(2, sum(lengths), np.complex64, "uniform")
+    return lengths, b, x
+
+
+def split(v, lengths):
+    out, o = [], 0
+    for n in lengths:
+        out.append(v[o:o + n])
+        o += n
+    return out
+
+
+@pytest.mark.parametrize("inverse", [False, True])
+def test_persistent_batch_matches_oracle_and_plain_path(batch, inverse):
+    lengths, b, x = batch
+    xd = torch.from_numpy(x).cuda()
+    y = torch.empty_like(xd)
+    b.execute(xd, y, invert=inverse)
+    assert b.status() == 0
+    y2 = torch.empty_like(xd)
+    b.execute_plain(xd, y2, invert=inverse)
+    torch.cuda.synchronize()
+    ys, y2s = split(y.cpu().numpy(), lengths), split(y2.cpu().numpy(), lengths)
+    for n, xi, yi, y2i in zip(lengths, split(x, lengths), ys, y2s):
+        ref = O.fft(xi, inverse=inverse)
+        assert O.rel_l2(yi, ref) <= 2e-6, n
+        assert O.rel_l2(yi, y2i) <= 2e-6, n
+
+
+def test_graph_replay_is_repeatable(batch):
+    lengths, b, x = batch
+    xd = torch.from_numpy(x).cuda()
+    y1, y2 = torch.empty_like(xd), torch.empty_like(xd)
+    b.execute(xd, y1)
+    b.execute(xd, y2)
+    assert b.status() == 0
+    assert torch.equal(y1, y2)
+
+
+def test_custom_offsets(batch):
+    lengths, b, x = batch
+    # pack the transforms in reverse order
+    offs, o = [0] * len(lengths), 0
+    for i in reversed(range(len(lengths))):
+        offs[i] = o
+        o += lengths[i]
+    xr = np.empty_like(x)
+    for i, xi in enumerate(split(x, lengths)):
+        xr[offs[i]:offs[i] + lengths[i]] = xi
+    xd = torch.from_numpy(xr).cuda()
+    y = torch.empty_like(xd)
+    off_d = torch.tensor(offs, dtype=torch.int64, device="cuda")
+    b.execute(xd, y, offsets_dev=off_d)
+    assert b.status() == 0
+    yh = y.cpu().numpy()
+    for i, xi in enumerate(split(x, lengths)):
+        assert O.rel_l2(yh[offs[i]:offs[i] + lengths[i]], O.fft(xi)) <= 2e-6
+
+
+def test_stalled_dependency_times_out_and_context_recovers(batch):
+    lengths, b, x = batch
+    xd = torch.from_numpy(x).cuda()
+    y = torch.empty_like(xd)
+    b.inject_stall(True, timeout_ms=200)
+    t0 = time.time()
+    b.execute(xd, y)
+    assert b.status() == 6          # FYG_ERR_TIMEOUT
+    assert time.time() - t0 < 10
+    b.inject_stall(False)
+    b.execute(xd, y)
+    assert b.status() == 0
+    ys = split(y.cpu().numpy(), lengths)
+    for n, xi, yi in zip(lengths[:32], split(x, lengths), ys):
+        assert O.rel_l2(yi, O.fft(xi)) <= 2e-6, n
