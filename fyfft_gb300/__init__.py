@@ -32,7 +32,7 @@ FYG_FLAG_CONV_FP64, FYG_FLAG_CONV_FP32, FYG_FLAG_NO_L2_CHUNK = 1, 2, 4
 
 # every symbol include/fygpu.h declares
 EXPORTED_SYMBOLS = (
-    "fyg_plan_create", "fyg_plan_destroy", "fyg_execute", "fyg_execute_adjoint", "fyg_strategy",
+    "fyg_plan_create", "fyg_plan_create_ex", "fyg_plan_destroy", "fyg_execute", "fyg_execute_adjoint", "fyg_strategy",
     "fyg_gpu_strategy", "fyg_plan_info", "fyg_plan_launches", "fyg_plan_profile",
     "fyg_plan_profile_read", "fyg_batch_create", "fyg_batch_destroy",
     "fyg_batch_execute", "fyg_batch_execute_plain", "fyg_batch_status", "fyg_batch_inject_stall",
@@ -69,6 +69,7 @@ def lib() -> ctypes.CDLL:
         L = ctypes.CDLL(LIB_PATH)
         sz, vp, i, d, u64 = ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_uint64
         L.fyg_plan_create.argtypes = [sz, i, sz, i, ctypes.POINTER(vp)]
+        L.fyg_plan_create_ex.argtypes = [sz, i, sz, i, sz, sz, ctypes.POINTER(vp)]
         L.fyg_plan_destroy.argtypes = [vp]
         L.fyg_execute.argtypes = [vp, vp, vp, i, vp]
         L.fyg_execute_adjoint.argtypes = [vp, vp, vp, d, vp]
@@ -158,12 +159,17 @@ class FFT1D_C2C_invoker:
 
     FFT_execution_strategy = FFT_execution_strategy
 
-    def __init__(self, length: int, dtype="complex64", batch: int = 1, flags: int = 0):
+    def __init__(self, length: int, dtype="complex64", batch: int = 1, flags: int = 0,
+                 max_pass_radix: int = 0, conv_length: int = 0):
         self.N = int(length)
         self.batch = int(batch)
         self.dtype_code = FYG_C32 if str(dtype).endswith("complex64") else FYG_C64
         h = ctypes.c_void_p()
-        check(lib().fyg_plan_create(self.N, self.dtype_code, self.batch, flags, ctypes.byref(h)))
+        if max_pass_radix or conv_length:
+            check(lib().fyg_plan_create_ex(self.N, self.dtype_code, self.batch, flags, int(max_pass_radix),
+                                           int(conv_length), ctypes.byref(h)))
+        else:
+            check(lib().fyg_plan_create(self.N, self.dtype_code, self.batch, flags, ctypes.byref(h)))
         self._h = h
 
     def close(self):

@@ -20,6 +20,7 @@
 // The reference's O(N^2) DFT fallback (src/foye_FFT_dft.hpp) is never used.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <map>
@@ -251,9 +252,15 @@ bool tile_fits(int cb, int R, int C, bool colmajor) {
 // Split L into P >= 2 pass radices whose C-column tiles fit in shared memory: fewest passes,
 // then fewest in-CTA stages, then the most balanced split.  For convolution pipelines the last
 // forward radix also runs the fused mid pass (two buffers).
+// Schedule overrides of fyg_plan_create_ex (0 = planner default), set for the duration of one
+// plan's creation.
+static thread_local uint64_t t_max_pass_r = 0;
+static thread_local uint64_t t_conv_len = 0;
+
 bool split_passes(uint64_t L, int cb, bool conv, std::vector<int>& out) {
     std::vector<int> divs;
-    for (int d = 4; d <= 4096 && (uint64_t)d <= L; ++d)
+    const int dmax = t_max_pass_r ? (int)std::min<uint64_t>(t_max_pass_r, 4096) : 4096;
+    for (int d = 4; d <= dmax && (uint64_t)d <= L; ++d)
         if (L % d == 0 && multi_C(cb, d)) divs.push_back(d);
     if (divs.empty()) return false;
     const int Rmax = divs.back();
@@ -546,9 +553,19 @@ static int make_plan(fyg_plan* pl) {
         ps.kind = GS_RADER;
         const uint64_t Lc = n - 1;
         ps.L = is_smooth(Lc, 13) ? Lc : next_smooth7(2 * Lc - 1);
+        if (t_conv_len) {
+            if (!(t_conv_len == Lc && is_smooth(Lc, 13)) && !(t_conv_len >= 2 * Lc - 1 && is_smooth(t_conv_len, 7)))
+                return set_error(FYG_ERR_INVALID_ARG, "Rader convolution length must be N-1 (13-smooth) or 7-smooth >= 2N-3");
+            ps.L = t_conv_len;
+        }
     } else {
         ps.kind = GS_BLUESTEIN;
         ps.L = next_smooth7(2 * n - 1);
+        if (t_conv_len) {
+            if (t_conv_len < 2 * n - 1 || !is_smooth(t_conv_len, 7))
+                return set_error(FYG_ERR_INVALID_ARG, "Bluestein convolution length must be 7-smooth and >= 2N-1");
+            ps.L = t_conv_len;
+        }
     }
     pl->strategy = ps.kind;
     pl->L = ps.L;
@@ -580,7 +597,12 @@ static int make_plan(fyg_plan* pl) {
     const int K = conv ? 2 * P - 1 : P;
     if (K == 1) pl->chunk = pl->batch;
     else {
-        const uint64_t chunk_elems = (32ull << 20) / cb;  // 32 MB per scratch buffer
+        // Whole batch per pass unless a scratch buffer would exceed 4 GB: measured on GB300, an
+        // L2-sized chunk (8-128 MB) is 1.1-1.5x slower than one launch per pass over the batch,
+        // because the tile kernels are issue-bound, not HBM-bound.  FYG_CHUNK_MB overrides.
+        uint64_t chunk_mb = 4096;
+        if (const char* e = std::getenv("FYG_CHUNK_MB")) chunk_mb = std::max<uint64_t>(1, std::strtoull(e, nullptr, 10));
+        const uint64_t chunk_elems = (chunk_mb << 20) / cb;
         uint64_t c = std::max<uint64_t>(1, chunk_elems / ps.L);
         if (pl->flags & FYG_FLAG_NO_L2_CHUNK) c = pl->batch;
         pl->chunk = (size_t)std::min<uint64_t>(c, pl->batch);
@@ -818,7 +840,14 @@ static int execute_dir(fyg_plan* pl, const void* in, void* out, bool inverse, do
 
 static int gpu_fft_f64(size_t n, const std::vector<double2>& h, std::vector<double2>& H) {
     fyg_plan* sub = nullptr;
+    const uint64_t keep_r = t_max_pass_r, keep_m = t_conv_len;
+    const int keep_cap = t_radix_cap;
+    t_max_pass_r = t_conv_len = 0;
+    t_radix_cap = 0;
     int rc = fyg_plan_create(n, FYG_C64, 1, 0, &sub);
+    t_max_pass_r = keep_r;
+    t_conv_len = keep_m;
+    t_radix_cap = keep_cap;
     if (rc) return rc;
     DevBuf a, b;
     rc = a.upload(h.data(), n * sizeof(double2));
@@ -846,6 +875,16 @@ fyg_plan::~fyg_plan() {
 }
 
 extern "C" {
+
+int fyg_plan_create_ex(size_t n, int dtype, size_t batch, int flags, size_t max_pass_radix, size_t conv_length,
+                       fyg_plan** out) {
+    t_max_pass_r = max_pass_radix;
+    t_conv_len = conv_length;
+    const int rc = fyg_plan_create(n, dtype, batch, flags, out);
+    t_max_pass_r = 0;
+    t_conv_len = 0;
+    return rc;
+}
 
 int fyg_plan_create(size_t n, int dtype, size_t batch, int flags, fyg_plan** out) {
     clear_error();

@@ -64,6 +64,13 @@ typedef struct fyg_batch fyg_batch;
  * the constructor's strategy choice and table/workspace set-up happen here, once. */
 int fyg_plan_create(size_t n, int dtype, size_t batch, int flags, fyg_plan** out);
 
+/* fyg_plan_create with schedule overrides (0 = the planner's default): max_pass_radix caps the
+ * radix of every multi-pass step; conv_length sets the Rader/Bluestein convolution length
+ * (Bluestein: 7-smooth >= 2N-1; Rader: N-1 when 13-smooth, or 7-smooth >= 2N-3).  Used by the
+ * autotuner; no counterpart in the reference. */
+int fyg_plan_create_ex(size_t n, int dtype, size_t batch, int flags, size_t max_pass_radix,
+                       size_t conv_length, fyg_plan** out);
+
 /* Releases the plan and its device tables and scratch. */
 int fyg_plan_destroy(fyg_plan* plan);
 
