@@ -108,8 +108,13 @@ class ClockSampler:
 # workloads
 # ----------------------------------------------------------------------------------------------
 
-def workload(name: str):
+def workload(name: str, sizes=None, batch=None):
     """[(n, batch, dtype, dist, seed)] and a description."""
+    if name == "sweep" and (sizes or batch):
+        sz = sizes or SWEEP_SIZES
+        b = batch or SWEEP_BATCH
+        return ([(n, b, "complex64", "normal", SEED) for n in sz],
+                f"sweep subset: complex<float> N in {sz} x batch {b}, N(0,1) seed 1")
     if name == "sweep":
         return ([(n, SWEEP_BATCH, "complex64", "normal", SEED) for n in SWEEP_SIZES],
                 "precision sweep: complex<float> N in {2520, 59049, 117649, 2^20, 1009, 65537, "
@@ -130,8 +135,22 @@ def run_ours(args, rank: int, world: int):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     stream = torch.cuda.current_stream()
-    items, desc = workload(args.workload)
+    items, desc = workload(args.workload, args.sizes, args.batch)
     hbm_peak, peak_src = peaks()
+
+    # schedule choice measured on this device before anything is timed (cached in a temp file)
+    if not args.no_autotune:
+        cache = args.autotune_cache or os.path.join(tempfile.gettempdir(),
+                                                    f"fyfft_gb300_bench_autotune_{os.getpid()}.json")
+        os.environ["FYG_AUTOTUNE_CACHE"] = cache
+        have = set()
+        if args.autotune_cache and os.path.exists(cache):
+            with open(cache) as f:
+                have = set(json.load(f).get("entries", {}))
+        for (n, batch, dt, *_ ) in items:
+            if f"{'c32' if dt == 'complex64' else 'c64'}:{n}" not in have:
+                fg.autotune(n, dt, batch, cache_path=cache)
+    plan_flags = 0 if args.no_autotune else fg.FYG_FLAG_AUTOTUNED
 
     plans, xin, yout, host_in, host_out = [], [], [], [], []
     for (n, batch, dt, dist, seed) in items:
@@ -143,7 +162,7 @@ def run_ours(args, rank: int, world: int):
         host_out.append(torch.empty_like(hx).pin_memory())
         xin.append(hx.to(f"cuda:{dev}"))
         yout.append(torch.empty(n * batch, dtype=tdt, device=f"cuda:{dev}"))
-        plans.append(fg.FFT1D_C2C_invoker(n, dt, batch))
+        plans.append(fg.FFT1D_C2C_invoker(n, dt, batch, flags=plan_flags))
     eb = [8 if dt == "complex64" else 16 for (_, _, dt, _, _) in items]
     step_flops = sum(flops(n) * b for (n, b, *_ ) in items)
     step_bytes = sum(2 * n * b * e for (n, b, *_), e in zip(items, eb))
@@ -176,7 +195,8 @@ def run_ours(args, rank: int, world: int):
         per_size[str(n)] = {"ms": round(ms, 4), "gflops": round(flops(n) * b / (ms * 1e-3) / 1e9, 1),
                             "gbs": round(gbs, 1), "hbm_frac": round(gbs / hbm_peak, 3),
                             "gpu_strategy": int(fg.FFT1D_C2C_invoker.gpu_execution_strategy(n)),
-                            "kernels": p.launches()}
+                            "kernels": p.launches(), "conv_length": p.info()["conv_length"],
+                            "passes": p.info()["passes"]}
 
     # headline: K steps, events on the launching stream, per-pass events for the roofline
     for p in plans:
@@ -247,7 +267,9 @@ def run_ours(args, rank: int, world: int):
         "data": "synthetic (seeded counter-based generator, fyg_fill_random)",
         "config": {"workload": desc, "sizes": [it[0] for it in items], "batch": [it[1] for it in items],
                    "l2": f"inputs larger than L2 ({in_bytes / 1e9:.2f} GB per step), no flush",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "schedules": "planner defaults" if args.no_autotune else
+                   "autotuned on this device before timing (fyg_autotune; conv length, pass radix, cols)"},
         "gbs": round(step_bytes * world / (ms_step * 1e-3) / 1e9, 1),
         "hbm_frac_step": round(step_bytes / (ms_step * 1e-3) / 1e9 / hbm_peak, 3),
         "roofline": roof,
@@ -345,7 +367,7 @@ def cpu_baseline(items, args, check=None):
 
 
 def run_reference(args, rank: int, world: int):
-    items, desc = workload(args.workload)
+    items, desc = workload(args.workload, args.sizes, args.batch)
     if rank != 0:
         return None
     from oracle import oracle as O
@@ -399,6 +421,12 @@ def main():
     ap.add_argument("--workload", default="sweep", choices=["sweep", "c1", "c5"])
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sizes", type=lambda v: [int(t) for t in v.split(",")], default=None,
+                    help="sweep subset (comma-separated lengths), for small profiling cases")
+    ap.add_argument("--batch", type=int, default=None, help="sweep batch override")
+    ap.add_argument("--autotune-cache", default=None,
+                    help="autotune cache file; tuning is skipped when it already holds every size")
+    ap.add_argument("--no-autotune", action="store_true", help="planner defaults instead of measured schedules")
     ap.add_argument("--no-uneven", action="store_true", help="skip the mixed-length batch comparison")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

@@ -29,10 +29,11 @@ FYG_OK = 0
 FYG_C32, FYG_C64 = 0, 1
 FYG_FORWARD, FYG_INVERSE = 1, -1
 FYG_FLAG_CONV_FP64, FYG_FLAG_CONV_FP32, FYG_FLAG_NO_L2_CHUNK = 1, 2, 4
+FYG_FLAG_SMALL_TILES, FYG_FLAG_AUTOTUNED = 8, 16
 
 # every symbol include/fygpu.h declares
 EXPORTED_SYMBOLS = (
-    "fyg_plan_create", "fyg_plan_create_ex", "fyg_plan_destroy", "fyg_execute", "fyg_execute_adjoint", "fyg_strategy",
+    "fyg_plan_create", "fyg_plan_create_ex", "fyg_autotune", "fyg_plan_destroy", "fyg_execute", "fyg_execute_adjoint", "fyg_strategy",
     "fyg_gpu_strategy", "fyg_plan_info", "fyg_plan_launches", "fyg_plan_profile",
     "fyg_plan_profile_read", "fyg_batch_create", "fyg_batch_destroy",
     "fyg_batch_execute", "fyg_batch_execute_plain", "fyg_batch_status", "fyg_batch_inject_stall",
@@ -70,6 +71,7 @@ def lib() -> ctypes.CDLL:
         sz, vp, i, d, u64 = ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_uint64
         L.fyg_plan_create.argtypes = [sz, i, sz, i, ctypes.POINTER(vp)]
         L.fyg_plan_create_ex.argtypes = [sz, i, sz, i, sz, sz, ctypes.POINTER(vp)]
+        L.fyg_autotune.argtypes = [sz, i, sz, ctypes.c_char_p, ctypes.POINTER(d)]
         L.fyg_plan_destroy.argtypes = [vp]
         L.fyg_execute.argtypes = [vp, vp, vp, i, vp]
         L.fyg_execute_adjoint.argtypes = [vp, vp, vp, d, vp]
@@ -93,6 +95,18 @@ def lib() -> ctypes.CDLL:
         L.fyg_version.restype = ctypes.c_char_p
         _lib = L
     return _lib
+
+
+def autotune(length: int, dtype="complex64", batch: int = 1, cache_path: str | None = None) -> float:
+    """Time the schedule candidates of one length on the current device and cache the fastest.
+
+    Plans created afterwards with flags=FYG_FLAG_AUTOTUNED use it.  Returns the winner's
+    milliseconds per forward batch."""
+    code = FYG_C32 if str(dtype).endswith("complex64") else FYG_C64
+    ms = ctypes.c_double()
+    path = cache_path.encode() if cache_path else None
+    check(lib().fyg_autotune(int(length), code, int(batch), path, ctypes.byref(ms)))
+    return ms.value
 
 
 def check(rc: int) -> None:

@@ -33,6 +33,16 @@ int pick_variant(int compute_cb, int tin_cb, int tout_cb, int cls);
 int threads_for(int R, int C, int maxt);
 void twiddle_ld(uint64_t t, uint64_t n, long double* c, long double* s);
 std::vector<unsigned char> host_local_table(int R, int cb);
+
+// Autotuner (fyg_autotune.cu): measured schedule choice per (dtype, length), cached in JSON.
+struct TuneChoice {
+    uint64_t max_pass_radix = 0, conv_length = 0;
+    int cols = 0;
+    double ms = 0;
+};
+bool tune_lookup(size_t n, int dtype, TuneChoice* out);
+int plan_create_opts(size_t n, int dtype, size_t batch, int flags, uint64_t max_pass_radix, uint64_t conv_length,
+                     int cols, fyg_plan** out);
 void host_two_level(uint64_t L, int cb, std::vector<unsigned char>& hi, std::vector<unsigned char>& lo, int* shift);
 
 // GPU-side strategy of a plan (what actually runs).

@@ -256,6 +256,7 @@ bool tile_fits(int cb, int R, int C, bool colmajor) {
 // plan's creation.
 static thread_local uint64_t t_max_pass_r = 0;
 static thread_local uint64_t t_conv_len = 0;
+static thread_local int t_cols = 0;   // single-pass: transforms per CTA (threads per transform = T/C)
 
 bool split_passes(uint64_t L, int cb, bool conv, std::vector<int>& out) {
     std::vector<int> divs;
@@ -588,10 +589,11 @@ static int make_plan(fyg_plan* pl) {
     if (P == 1) {
         // several transforms per CTA for small lengths
         const int target = cb == 8 ? 4096 : 2048;
-        int C = std::max(1, target / (int)ps.L);
+        int C = t_cols ? t_cols : std::max(1, target / (int)ps.L);
         C = (int)std::min<uint64_t>((uint64_t)C, pl->batch);
         C = std::min(C, 256);
         ps.C = std::max(C, 1);
+        if (smem_for(cb, (int)ps.L, ps.C, true) > kSmemLimit) ps.C = 1;
     }
     // ---- chunking: keep the scratch of one chunk L2-resident ----
     const int K = conv ? 2 * P - 1 : P;
@@ -841,13 +843,14 @@ static int execute_dir(fyg_plan* pl, const void* in, void* out, bool inverse, do
 static int gpu_fft_f64(size_t n, const std::vector<double2>& h, std::vector<double2>& H) {
     fyg_plan* sub = nullptr;
     const uint64_t keep_r = t_max_pass_r, keep_m = t_conv_len;
-    const int keep_cap = t_radix_cap;
+    const int keep_cap = t_radix_cap, keep_cols = t_cols;
     t_max_pass_r = t_conv_len = 0;
-    t_radix_cap = 0;
+    t_radix_cap = t_cols = 0;
     int rc = fyg_plan_create(n, FYG_C64, 1, 0, &sub);
     t_max_pass_r = keep_r;
     t_conv_len = keep_m;
     t_radix_cap = keep_cap;
+    t_cols = keep_cols;
     if (rc) return rc;
     DevBuf a, b;
     rc = a.upload(h.data(), n * sizeof(double2));
@@ -874,20 +877,37 @@ fyg_plan::~fyg_plan() {
     for (cudaEvent_t e : prof_pool) cudaEventDestroy(e);
 }
 
+namespace fyg {
+// plan creation with explicit schedule options (0 = default); used by the autotuner
+int plan_create_opts(size_t n, int dtype, size_t batch, int flags, uint64_t max_pass_radix, uint64_t conv_length,
+                     int cols, fyg_plan** out) {
+    t_max_pass_r = max_pass_radix;
+    t_conv_len = conv_length;
+    t_cols = cols;
+    const int rc = fyg_plan_create(n, dtype, batch, flags & ~FYG_FLAG_AUTOTUNED, out);
+    t_max_pass_r = 0;
+    t_conv_len = 0;
+    t_cols = 0;
+    return rc;
+}
+}  // namespace fyg
+
 extern "C" {
 
 int fyg_plan_create_ex(size_t n, int dtype, size_t batch, int flags, size_t max_pass_radix, size_t conv_length,
                        fyg_plan** out) {
-    t_max_pass_r = max_pass_radix;
-    t_conv_len = conv_length;
-    const int rc = fyg_plan_create(n, dtype, batch, flags, out);
-    t_max_pass_r = 0;
-    t_conv_len = 0;
-    return rc;
+    return plan_create_opts(n, dtype, batch, flags & ~FYG_FLAG_AUTOTUNED, max_pass_radix, conv_length, 0, out);
 }
+
 
 int fyg_plan_create(size_t n, int dtype, size_t batch, int flags, fyg_plan** out) {
     clear_error();
+    if (flags & FYG_FLAG_AUTOTUNED) {
+        TuneChoice tc;
+        if (tune_lookup(n, dtype, &tc)) return plan_create_opts(n, dtype, batch, flags, tc.max_pass_radix,
+                                                                tc.conv_length, tc.cols, out);
+        flags &= ~FYG_FLAG_AUTOTUNED;
+    }
     if (!out) return set_error(FYG_ERR_NULL_PTR, "out is null");
     *out = nullptr;
     if (n < 1) return set_error(FYG_ERR_INVALID_LENGTH, "length must be >= 1");

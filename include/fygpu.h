@@ -55,6 +55,7 @@ extern "C" {
 #define FYG_FLAG_CONV_FP32 0x2   /* force the FP32 convolution (disables the error-budget choice) */
 #define FYG_FLAG_NO_L2_CHUNK 0x4 /* process the whole batch per pass (no L2-resident chunking) */
 #define FYG_FLAG_SMALL_TILES 0x8 /* single-CTA transforms up to ~100 KB of shared memory, stage radix <= 16 */
+#define FYG_FLAG_AUTOTUNED 0x10  /* use the autotuner's cached schedule for this length, if any */
 
 typedef struct fyg_plan fyg_plan;
 typedef struct fyg_batch fyg_batch;
@@ -70,6 +71,15 @@ int fyg_plan_create(size_t n, int dtype, size_t batch, int flags, fyg_plan** out
  * autotuner; no counterpart in the reference. */
 int fyg_plan_create_ex(size_t n, int dtype, size_t batch, int flags, size_t max_pass_radix,
                        size_t conv_length, fyg_plan** out);
+
+/* Autotuner (no counterpart in the reference): times candidate schedules for one length on the
+ * current device -- convolution lengths (Rader/Bluestein), caps on the pass radix (multi-pass),
+ * transforms per CTA (single-pass, i.e. threads per transform) -- and stores the fastest in the
+ * JSON cache at `cache_path` (NULL: $FYG_AUTOTUNE_CACHE, else ~/.cache/fyfft_gb300/autotune.json),
+ * keyed by device name, SM count, compute capability and driver.  `batch` is the batch the
+ * candidates are timed with.  Plans created with FYG_FLAG_AUTOTUNED use the cached choice.
+ * *best_ms (optional) receives the winner's time per forward batch. */
+int fyg_autotune(size_t n, int dtype, size_t batch, const char* cache_path, double* best_ms);
 
 /* Releases the plan and its device tables and scratch. */
 int fyg_plan_destroy(fyg_plan* plan);
