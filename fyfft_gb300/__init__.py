@@ -29,12 +29,12 @@ FYG_OK = 0
 FYG_C32, FYG_C64 = 0, 1
 FYG_FORWARD, FYG_INVERSE = 1, -1
 FYG_FLAG_CONV_FP64, FYG_FLAG_CONV_FP32, FYG_FLAG_NO_L2_CHUNK = 1, 2, 4
-FYG_FLAG_SMALL_TILES, FYG_FLAG_AUTOTUNED = 8, 16
+FYG_FLAG_SMALL_TILES, FYG_FLAG_AUTOTUNED, FYG_FLAG_GENERIC_KERNELS = 8, 16, 32
 
 # every symbol include/fygpu.h declares
 EXPORTED_SYMBOLS = (
     "fyg_plan_create", "fyg_plan_create_ex", "fyg_autotune", "fyg_plan_destroy", "fyg_execute", "fyg_execute_adjoint", "fyg_strategy",
-    "fyg_gpu_strategy", "fyg_plan_info", "fyg_plan_launches", "fyg_plan_profile",
+    "fyg_gpu_strategy", "fyg_plan_info", "fyg_plan_launches", "fyg_plan_describe", "fyg_plan_profile",
     "fyg_plan_profile_read", "fyg_batch_create", "fyg_batch_destroy",
     "fyg_batch_execute", "fyg_batch_execute_plain", "fyg_batch_status", "fyg_batch_inject_stall",
     "fyg_execute_noalloc", "fyg_last_error_string",
@@ -79,6 +79,7 @@ def lib() -> ctypes.CDLL:
         L.fyg_gpu_strategy.argtypes = [sz]
         L.fyg_plan_info.argtypes = [vp, ctypes.POINTER(sz), ctypes.POINTER(i), ctypes.POINTER(i)]
         L.fyg_plan_launches.argtypes = [vp, ctypes.POINTER(i)]
+        L.fyg_plan_describe.argtypes = [vp, ctypes.c_char_p, sz]
         L.fyg_plan_profile.argtypes = [vp, i]
         L.fyg_plan_profile_read.argtypes = [vp, ctypes.POINTER(d), ctypes.POINTER(ctypes.c_int64),
                                             ctypes.POINTER(ctypes.c_int64), i, ctypes.POINTER(i)]
@@ -228,6 +229,12 @@ class FFT1D_C2C_invoker:
         L, P, S = ctypes.c_size_t(), ctypes.c_int(), ctypes.c_int()
         check(lib().fyg_plan_info(self._h, ctypes.byref(L), ctypes.byref(P), ctypes.byref(S)))
         return {"conv_length": L.value, "passes": P.value, "gpu_strategy": S.value}
+
+    def describe(self) -> list[str]:
+        """One line per forward pass: kernel kind, tile shape and fusions."""
+        buf = ctypes.create_string_buffer(8192)
+        check(lib().fyg_plan_describe(self._h, buf, len(buf)))
+        return buf.value.decode().splitlines()
 
     def launches(self) -> int:
         n = ctypes.c_int()

@@ -3,8 +3,8 @@
 // For one length the candidates are the knobs the planner otherwise sets by rule:
 //   single-pass lengths   transforms per CTA (C), i.e. threads per transform = threads / C
 //   multi-pass lengths    a cap on the pass radix (more, smaller passes or fewer, larger ones)
-//   Rader / Bluestein     the convolution length (7-smooth lengths up to 8% above the minimum)
-//                         and a cap on its pass radix
+//   Rader / Bluestein     the convolution length (7-smooth lengths up to 8% above the minimum,
+//                         and for Bluestein the power of two) and a cap on its pass radix
 // Every candidate plan runs a forward batch on the current device (CUDA events, best of three
 // after a warm-up); the fastest is written to the cache under "c32:<n>" / "c64:<n>" together
 // with the device signature (name, SM count, compute capability, driver).  A cache written
@@ -13,6 +13,7 @@
 
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <fstream>
 #include <map>
@@ -147,7 +148,12 @@ std::vector<TuneChoice> candidates(size_t n, int dtype, size_t batch) {
     std::vector<uint64_t> ms;
     if (prime(n) && smooth(n - 1, 13)) ms.push_back(n - 1);
     else if (prime(n) && 2 * n - 3 <= 78125) ms = smooth7_from(2 * n - 3, 6, 1.08);
-    else ms = smooth7_from(2 * n - 1, 8, 1.08);
+    else {
+        ms = smooth7_from(2 * n - 1, 8, 1.08);
+        uint64_t m2 = 1;
+        while (m2 < 2 * n - 1) m2 <<= 1;
+        if (std::find(ms.begin(), ms.end(), m2) == ms.end()) ms.push_back(m2);
+    }
     for (uint64_t m : ms)
         for (uint64_t r : {0ull, 256ull}) add(r, m, 0);
     return out;

@@ -1,0 +1,250 @@
+// fyg_fast.cuh -- register-resident tile-pass kernels for power-of-two tile lengths (FP32).
+//
+// Same pass algebra as fyg_pass.cuh (one radix-R Stockham step of a length-L transform over C
+// consecutive columns), with the in-CTA length-R DFT organised around registers instead of
+// shared-memory sweeps:
+//   * a column is served by G = R/P threads; thread g of column c owns the P points
+//     n = g + G*i (i < P) and keeps them in registers for the whole pass;
+//   * stage s (radix r = min(P, R/P^s), ns = P^s) is P/r butterflies per thread whose operands
+//     are exactly those registers (j = g + G*b, inputs j + m*R/r = g + G*(b + m*P/r)), so the
+//     global load feeds the first butterflies directly and the last stage leaves output point
+//     n = g + G*i in register i (Stockham order is natural order at the end);
+//   * between stages the outputs go through one shared buffer (column-major, padded so that
+//     both the strided writes and the unit-stride reads are free of bank conflicts);
+//   * the store is direct and coalesced across the tile's columns when the output stride
+//     Ns_out > 1, and a flat copy through shared memory when Ns_out = 1 (the tile's columns are
+//     then back to back in memory).
+// Columns per tile C and points per thread P are chosen per R so that a CTA has 256 threads and
+// two CTAs fit on an SM (<= 128 registers per thread, one shared buffer): one CTA's loads
+// overlap the other's butterflies.
+//
+// Fusions: conjugation and the inter-pass twiddle (two-level table), the Bluestein chirp with
+// zero padding or the Rader gather at the load; the fused mid pass of a convolution (spectrum
+// multiply, conjugation, second in-CTA DFT = first inverse pass, Rader DC capture); scaling,
+// conjugation, the Bluestein output chirp with truncation or the Rader scatter with the x0 and
+// DC terms at the store.  Uneven batches use the generic kernel (fyg_kernels.cuh).
+#pragma once
+#include "fyg_pass.cuh"
+
+namespace fyg {
+
+// Shape of a fast tile: R points per column, P registers-points per thread, C columns per tile.
+template <int R_, int P_, int C_> struct FastShape {
+    static constexpr int R = R_, P = P_, C = C_;
+    static constexpr int G = R / P;            // threads per column
+    static constexpr int T = C * G;            // threads per CTA
+    __host__ __device__ static constexpr int pad(int n) { return n >> 5; }
+    // pitch of a column: >= R + R/32 and = 16/C (mod 16) (8-byte words), so the C columns of a
+    // half-warp start in different banks
+    static constexpr int Rp = ((R + (R >> 5) + 15) & ~15) + 16 / C;
+    __host__ __device__ static constexpr int nst() {
+        int s = 0;
+        for (int rem = R; rem > 1; rem /= (rem < P ? rem : P)) ++s;
+        return s;
+    }
+    __host__ __device__ static constexpr int radix(int s) {
+        int rem = R;
+        for (int t = 0; t < s; ++t) rem /= (rem < P ? rem : P);
+        return rem < P ? rem : P;
+    }
+    __host__ __device__ static constexpr int ns(int s) {
+        int v = 1;
+        for (int t = 0; t < s; ++t) v *= radix(t);
+        return v;
+    }
+    static constexpr size_t smem_bytes() { return (size_t)C * Rp * sizeof(float2); }
+};
+
+template <class S> __device__ __forceinline__ int fast_addr(int c, int n) { return c * S::Rp + n + S::pad(n); }
+
+// One in-CTA Stockham stage over the thread's registers.  Non-final stages write their outputs
+// to shared memory and read the next stage's operands back (two barriers: the buffer is shared
+// by consecutive exchanges).
+template <class S, int ST>
+__device__ __forceinline__ void fast_stage(float2 (&v)[S::P], float2* sm, int c, int g, const float2* twl) {
+    constexpr int r = S::radix(ST), ns = S::ns(ST), nb = S::P / r;
+    constexpr bool last = ST == S::nst() - 1;
+    constexpr int twm = S::R / (ns * r);
+#pragma unroll
+    for (int b = 0; b < nb; ++b) {
+        float2 x[r];
+#pragma unroll
+        for (int m = 0; m < r; ++m) x[m] = v[b + m * nb];
+        const int j = g + S::G * b;
+        const int k = j & (ns - 1);
+        if constexpr (ST > 0) {
+            if (k) {
+                const int t = k * twm;
+#pragma unroll
+                for (int m = 1; m < r; ++m) x[m] = cmul(x[m], __ldg(twl + m * t));
+            }
+        }
+        dft<r, float>(x);
+        if constexpr (last) {
+#pragma unroll
+            for (int m = 0; m < r; ++m) v[b + m * nb] = x[m];
+        } else {
+            const int base = (j - k) * r + k;   // (j / ns) * ns * r + k
+#pragma unroll
+            for (int m = 0; m < r; ++m) sm[fast_addr<S>(c, base + m * ns)] = x[m];
+        }
+    }
+    if constexpr (!last) {
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < S::P; ++i) v[i] = sm[fast_addr<S>(c, g + S::G * i)];
+        __syncthreads();
+    }
+}
+
+template <class S, int ST>
+__device__ __forceinline__ void fast_stages_from(float2 (&v)[S::P], float2* sm, int c, int g, const float2* twl) {
+    if constexpr (ST < S::nst()) {
+        fast_stage<S, ST>(v, sm, c, g, twl);
+        fast_stages_from<S, ST + 1>(v, sm, c, g, twl);
+    }
+}
+
+template <class S>
+__global__ void __launch_bounds__(S::T, (S::T <= 256 ? 2 : 1)) k_fast(const __grid_constant__ PassParams p) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    float2* sm = reinterpret_cast<float2*>(smraw);
+    constexpr int P = S::P, G = S::G, C = S::C, R = S::R;
+    const int c = threadIdx.x & (C - 1);
+    const int g = threadIdx.x / C;
+    // all C columns of a tile belong to one transform (Rr is a multiple of C)
+    const Col<float> ci = make_col<float, float>(p, (int64_t)blockIdx.x * C + c);
+    const float2* twl = reinterpret_cast<const float2*>(p.tw_local);
+    const int Rr = p.Rr;
+
+    // ---- load: register i <- x[jj + n Rr], n = g + G i ----
+    float2 v[P];
+    {
+        const float2* src = reinterpret_cast<const float2*>(p.in) + ci.in_base + ci.jj;
+        if (p.load_mode == LD_CHIRP) {
+            const float2* chirp = reinterpret_cast<const float2*>(p.chirp);
+            const int64_t nvalid = p.nvalid;
+#pragma unroll
+            for (int i = 0; i < P; ++i) {
+                const int gidx = ci.jj + (g + G * i) * Rr;
+                v[i] = make_float2(0.f, 0.f);
+                if (gidx < nvalid) v[i] = ld_data(src + (g + G * i) * Rr);
+            }
+#pragma unroll
+            for (int i = 0; i < P; ++i) {
+                const int gidx = ci.jj + (g + G * i) * Rr;
+                if (gidx < nvalid) {
+                    float2 u = v[i];
+                    if (p.conj_in) u.y = -u.y;
+                    v[i] = cmul(u, cconj(__ldg(chirp + gidx)));
+                }
+            }
+        } else if (p.load_mode == LD_GATHER) {
+            // Rader: x[gather[n]] (gather < 0: zero padding); the transform's x[0] is saved
+            const float2* base = reinterpret_cast<const float2*>(p.in) + ci.in_base;
+            const int* gather = p.gather;
+#pragma unroll
+            for (int i = 0; i < P; ++i) {
+                const int t = __ldg(gather + ci.jj + (g + G * i) * Rr);
+                v[i] = t >= 0 ? ld_data(base + t) : make_float2(0.f, 0.f);
+            }
+            if (p.conj_in) {
+#pragma unroll
+                for (int i = 0; i < P; ++i) v[i].y = -v[i].y;
+            }
+            if (p.x0_from_in && p.x0buf && ci.jj == 0 && g == 0)
+                reinterpret_cast<float2*>(p.x0buf)[ci.b] = ld_data(base);
+        } else {
+#pragma unroll
+            for (int i = 0; i < P; ++i) v[i] = ld_data(src + (g + G * i) * Rr);
+            const float isign = p.conj_in ? -1.f : 1.f;
+            if (p.Ns > 1 && ci.k) {
+                const uint32_t kL = (uint32_t)ci.k * (uint32_t)p.Lr;
+#pragma unroll
+                for (int i = 0; i < P; ++i) {
+                    const uint32_t e = (uint32_t)(g + G * i) * kL;
+                    float2 u = v[i];
+                    u.y *= isign;
+                    v[i] = e ? cmul(u, tw_two_level(p.tw_hi, p.tw_lo, p.tw_shift, e, 0.f)) : u;
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < P; ++i) v[i].y *= isign;
+            }
+        }
+    }
+
+    fast_stages_from<S, 0>(v, sm, c, g, twl);
+
+    if (p.mid) {
+        // forward output point n of this column is global index jj + n Rr of the convolution
+        const float2* spec = reinterpret_cast<const float2*>(p.spectrum);
+        // Rader: the DC term of the forward convolution FFT (global index 0 = register 0 of
+        // thread 0 of column 0)
+        if (p.dc_capture && ci.jj == 0 && g == 0) reinterpret_cast<float2*>(p.dcbuf)[ci.b] = v[0];
+#pragma unroll
+        for (int i = 0; i < P; ++i) v[i] = cconj(cmul(v[i], __ldg(spec + ci.jj + (g + G * i) * Rr)));
+        fast_stages_from<S, 0>(v, sm, c, g, twl);
+    }
+
+    // ---- store ----
+    const float scale = (float)p.scale;
+    if (p.Ns_out == 1) {
+        // the tile's C columns are C consecutive length-R runs of the output: flat copy
+        const float sy = p.conj_out ? -scale : scale;
+#pragma unroll
+        for (int i = 0; i < P; ++i) sm[fast_addr<S>(c, g + G * i)] = v[i];
+        __syncthreads();
+        const int64_t jj0 = ci.jj - c;
+        float2* dst = reinterpret_cast<float2*>(p.out) + ci.out_base + jj0 * R;
+#pragma unroll 4
+        for (int e = threadIdx.x; e < C * R; e += S::T) {
+            const float2 u = sm[fast_addr<S>(e / R, e & (R - 1))];
+            dst[e] = make_float2(u.x * scale, u.y * sy);
+        }
+    } else {
+        float2* dst = reinterpret_cast<float2*>(p.out) + ci.out_base + ci.out_j;
+        const int ns = p.Ns_out;
+        if (p.store_mode == ST_CHIRP) {
+            const float2* chirp = reinterpret_cast<const float2*>(p.chirp);
+            const int64_t nvalid = p.nvalid;
+#pragma unroll
+            for (int i = 0; i < P; ++i) {
+                const int oidx = ci.out_j + (g + G * i) * ns;
+                if (oidx < nvalid) {
+                    float2 u = cscale(cmul(__ldg(chirp + oidx), v[i]), scale);
+                    if (p.conj_out) u.y = -u.y;
+                    dst[(g + G * i) * ns] = u;
+                }
+            }
+        } else if (p.store_mode == ST_SCATTER) {
+            // Rader: out[scatter[k]] = (x0 + y*scale (conjugated forward)) * scale2, and the DC
+            // term out[0] = (x0 + A0) * scale2 with A0 the forward convolution's DC term
+            float2* obase = reinterpret_cast<float2*>(p.out) + ci.out_base;
+            const float2 x0 = ld_data(reinterpret_cast<const float2*>(p.x0buf) + ci.b);
+            const float scale2 = (float)p.scale2;
+            const int* scatter = p.scatter;
+#pragma unroll
+            for (int i = 0; i < P; ++i) {
+                const int oidx = ci.out_j + (g + G * i) * ns;
+                if (oidx == 0) {
+                    float2 a0 = ld_data(reinterpret_cast<const float2*>(p.dcbuf) + ci.b);
+                    if (!p.conj_out) a0.y = -a0.y;
+                    obase[0] = cscale(cadd(x0, a0), scale2);
+                }
+                const int t = __ldg(scatter + oidx);
+                if (t > 0) {
+                    float2 u = cscale(v[i], scale);
+                    if (p.conj_out) u.y = -u.y;
+                    obase[t] = cscale(cadd(x0, u), scale2);
+                }
+            }
+        } else {
+            const float sy = p.conj_out ? -scale : scale;
+#pragma unroll
+            for (int i = 0; i < P; ++i) dst[(g + G * i) * ns] = make_float2(v[i].x * scale, v[i].y * sy);
+        }
+    }
+}
+
+}  // namespace fyg

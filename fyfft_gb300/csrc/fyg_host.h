@@ -110,6 +110,10 @@ struct fyg_plan {
     fyg::DevBuf scratch0, scratch1, x0buf, dcbuf, errword;
     fyg::DevBuf stage_in, stage_out;   // staging for host pointers
     size_t stage_in_bytes = 0;
+    // host-pointer execution: copy-in and copy-out streams and per-chunk events, so that the
+    // copies of one batch chunk overlap the kernels of the previous one
+    cudaStream_t s_h2d = nullptr, s_d2h = nullptr;
+    std::vector<cudaEvent_t> stage_ev;
     // instrumentation: event pairs per launch, accumulated per forward pass
     bool profile = false;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;

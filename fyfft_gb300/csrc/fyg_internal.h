@@ -16,6 +16,7 @@ enum KernelVariant : int {
     KV_F64_IF32_C16,    // double compute, float in,  double out
     KV_F64_OF32_C16,    // double compute, double in, float out
     KV_F64_F32IO_C16,   // double compute, float in,  float out
+    KV_FAST,            // register-resident FP32 kernel of a power-of-two tile length (fyg_fast.cuh)
     KV_COUNT
 };
 
@@ -25,6 +26,10 @@ VariantInfo variant_info(int kv);
 // Launches one tile pass; sets the dynamic shared-memory attribute when needed.
 cudaError_t launch_pass(int kv, const PassParams& p, unsigned grid, int threads, size_t smem,
                         cudaStream_t st);
+
+// Register-resident kernels: the tile shape for R (false if R has none) and the launch.
+bool fast_shape(int R, int* C, int* threads, size_t* smem);
+cudaError_t launch_fast(const PassParams& p, unsigned grid, cudaStream_t st);
 
 // Uploads the codelet constant tables to the current device (once per device).
 cudaError_t ensure_device_constants();

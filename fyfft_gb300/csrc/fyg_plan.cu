@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <cstdio>
 #include <cstring>
 #include <functional>
 #include <map>
@@ -38,10 +39,11 @@ cudaError_t launch_scale_copy(const void* in, void* out, size_t n, int dtype, do
                               cudaStream_t st);
 
 VariantInfo variant_info(int kv) {
-    return {512, (kv == KV_F32_C16 || kv == KV_F32_C32) ? 8 : 16};
+    return {512, (kv == KV_F32_C16 || kv == KV_F32_C32 || kv == KV_FAST) ? 8 : 16};
 }
 
 cudaError_t launch_pass(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st) {
+    if (kv == KV_FAST) return launch_fast(p, grid, st);
     if (kv == KV_F32_C16) return launch_f32(kv, p, grid, threads, smem, st);
     if (kv == KV_F32_C32) return launch_f32c32(kv, p, grid, threads, smem, st);
     if (kv == KV_F64_C16) return launch_f64(kv, p, grid, threads, smem, st);
@@ -512,6 +514,18 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
         d.threads = threads_for(R, C, kMaxThreads);
         d.kv = pick_variant(cb, (int)d.in_elem_bytes, (int)d.out_elem_bytes, cls);
         d.smem = smem_for(cb, R, C, single);
+        // register-resident kernel for power-of-two tiles of FP32 passes (not for the tiles of
+        // uneven batches, which run inside the generic persistent kernel)
+        int fc = 0, ft = 0;
+        size_t fsm = 0;
+        if (pl->dtype == FYG_C32 && cb == 8 && !single &&
+            !(pl->flags & (FYG_FLAG_SMALL_TILES | FYG_FLAG_GENERIC_KERNELS)) && fast_shape(R, &fc, &ft, &fsm) &&
+            (L / R) % (uint64_t)fc == 0) {
+            fill_geom(p.g, R, fc, false, rad);
+            d.kv = KV_FAST;
+            d.threads = ft;
+            d.smem = fsm;
+        }
         if (d.smem > kSmemLimit)
             return set_error(FYG_ERR_UNSUPPORTED, "tile of " + std::to_string(R) + "x" + std::to_string(C) +
                                                       " exceeds shared memory");
@@ -562,6 +576,13 @@ static int make_plan(fyg_plan* pl) {
     } else {
         ps.kind = GS_BLUESTEIN;
         ps.L = next_smooth7(2 * n - 1);
+        // FP32 multi-pass convolutions: the power-of-two length runs on the register-resident
+        // kernels, which more than make up for up to twice the points
+        uint64_t m2 = 1;
+        while (m2 < 2 * n - 1) m2 <<= 1;
+        if (pl->dtype == FYG_C32 && m2 >= 65536 &&
+            !(pl->flags & (FYG_FLAG_CONV_FP64 | FYG_FLAG_SMALL_TILES | FYG_FLAG_GENERIC_KERNELS)))
+            ps.L = m2;
         if (t_conv_len) {
             if (t_conv_len < 2 * n - 1 || !is_smooth(t_conv_len, 7))
                 return set_error(FYG_ERR_INVALID_ARG, "Bluestein convolution length must be 7-smooth and >= 2N-1");
@@ -734,11 +755,13 @@ static int make_plan(fyg_plan* pl) {
 // Execution
 // ------------------------------------------------------------------------------------------
 
+// Runs the pipeline over transforms [b_begin, b_end) of the batch (in/out are the batch bases).
 static int run_pipeline(fyg_plan* pl, const std::vector<PassDesc>& pipe, const void* in, void* out,
-                        double final_scale_mul, cudaStream_t st) {
+                        double final_scale_mul, cudaStream_t st, size_t b_begin = 0, size_t b_end = SIZE_MAX) {
     const int io_cb = pl->dtype == FYG_C32 ? 8 : 16;
-    for (size_t c0 = 0; c0 < pl->batch; c0 += pl->chunk) {
-        const size_t nb = std::min(pl->chunk, pl->batch - c0);
+    b_end = std::min(b_end, pl->batch);
+    for (size_t c0 = b_begin; c0 < b_end; c0 += pl->chunk) {
+        const size_t nb = std::min(pl->chunk, b_end - c0);
         for (size_t i = 0; i < pipe.size(); ++i) {
             const PassDesc& d = pipe[i];
             PassParams p = d.p;
@@ -793,6 +816,68 @@ static bool is_device_ptr(const void* ptr) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Host input and output: the batch is cut into chunks; chunk i's host->device copy (copy-in
+// stream), its kernels (the caller's stream) and its device->host copy (copy-out stream) are
+// ordered by events, so copies in both directions overlap the kernels of neighbouring chunks.
+// Returns when the output is in host memory.
+static int execute_host_overlapped(fyg_plan* pl, const void* in, void* out, bool inverse, double scale_mul,
+                                   cudaStream_t st) {
+    const int io_cb = pl->dtype == FYG_C32 ? 8 : 16;
+    const size_t per = pl->n * (size_t)io_cb;
+    const size_t bytes = per * pl->batch;
+    int rc = FYG_OK;
+    if (pl->stage_in_bytes < bytes) {
+        rc = pl->stage_in.alloc(bytes);
+        if (!rc) rc = pl->stage_out.alloc(bytes);
+        if (rc) return rc;
+        pl->stage_in_bytes = bytes;
+    }
+    // about 8 chunks, whole transforms, at least one L2 chunk of the plan each
+    size_t cb = std::max<size_t>((pl->batch + 7) / 8, 1);
+    if (pl->chunk < pl->batch) cb = std::max(cb, pl->chunk) / pl->chunk * pl->chunk;
+    const size_t nch = (pl->batch + cb - 1) / cb;
+    if (!pl->s_h2d) {
+        cudaError_t e = cudaStreamCreateWithFlags(&pl->s_h2d, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pl->s_d2h, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return cuda_error(e, "staging streams");
+    }
+    while (pl->stage_ev.size() < 2 * nch + 1) {
+        cudaEvent_t ev;
+        cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_error(e, "staging events");
+        pl->stage_ev.push_back(ev);
+    }
+    cudaEvent_t start = pl->stage_ev[2 * nch];
+    auto chk = [&](cudaError_t e, const char* what) { return e == cudaSuccess ? FYG_OK : cuda_error(e, what); };
+    // earlier work on the caller's stream may still read the staging buffers
+    rc = chk(cudaEventRecord(start, st), "event");
+    if (!rc) rc = chk(cudaStreamWaitEvent(pl->s_h2d, start, 0), "wait");
+    const char* hin = static_cast<const char*>(in);
+    char* hout = static_cast<char*>(out);
+    char* sin = static_cast<char*>(pl->stage_in.ptr);
+    char* sout = static_cast<char*>(pl->stage_out.ptr);
+    for (size_t i = 0; i < nch && !rc; ++i) {
+        const size_t b0 = i * cb, nb = std::min(cb, pl->batch - b0);
+        cudaEvent_t ev_in = pl->stage_ev[2 * i], ev_done = pl->stage_ev[2 * i + 1];
+        rc = chk(cudaMemcpyAsync(sin + b0 * per, hin + b0 * per, nb * per, cudaMemcpyHostToDevice, pl->s_h2d),
+                 "host->device staging");
+        if (!rc) rc = chk(cudaEventRecord(ev_in, pl->s_h2d), "event");
+        if (!rc) rc = chk(cudaStreamWaitEvent(st, ev_in, 0), "wait");
+        if (!rc) rc = run_pipeline(pl, inverse ? pl->inv : pl->fwd, sin, sout, scale_mul, st, b0, b0 + nb);
+        if (!rc) rc = chk(cudaEventRecord(ev_done, st), "event");
+        if (!rc) rc = chk(cudaStreamWaitEvent(pl->s_d2h, ev_done, 0), "wait");
+        if (!rc)
+            rc = chk(cudaMemcpyAsync(hout + b0 * per, sout + b0 * per, nb * per, cudaMemcpyDeviceToHost, pl->s_d2h),
+                     "device->host staging");
+    }
+    // always drain both copy streams before returning (the host buffers are the caller's)
+    const cudaError_t e1 = cudaStreamSynchronize(pl->s_h2d);
+    const cudaError_t e2 = cudaStreamSynchronize(pl->s_d2h);
+    if (!rc) rc = chk(e1, "stream synchronize");
+    if (!rc) rc = chk(e2, "stream synchronize");
+    return rc;
+}
+
 static int execute_dir(fyg_plan* pl, const void* in, void* out, bool inverse, double scale_mul, cudaStream_t st) {
     if (!pl) return set_error(FYG_ERR_NULL_PTR, "null plan");
     if (!in || !out) return set_error(FYG_ERR_NULL_PTR, "null buffer");
@@ -804,6 +889,11 @@ static int execute_dir(fyg_plan* pl, const void* in, void* out, bool inverse, do
     if (cur != pl->device) cudaSetDevice(pl->device);
     const size_t bytes = pl->n * pl->batch * io_cb;
     const bool din = is_device_ptr(in), dout = is_device_ptr(out);
+    if (!din && !dout && pl->strategy != GS_COPY && pl->batch >= 2 && bytes >= (8u << 20)) {
+        const int rc = execute_host_overlapped(pl, in, out, inverse, scale_mul, st);
+        if (cur != pl->device) cudaSetDevice(cur);
+        return rc;
+    }
     const void* din_p = in;
     void* dout_p = out;
     int rc = FYG_OK;
@@ -875,6 +965,9 @@ using namespace fyg;
 
 fyg_plan::~fyg_plan() {
     for (cudaEvent_t e : prof_pool) cudaEventDestroy(e);
+    for (cudaEvent_t e : stage_ev) cudaEventDestroy(e);
+    if (s_h2d) cudaStreamDestroy(s_h2d);
+    if (s_d2h) cudaStreamDestroy(s_d2h);
 }
 
 namespace fyg {
@@ -945,6 +1038,26 @@ int fyg_plan_launches(const fyg_plan* plan, int* launches) {
     if (!plan || !launches) return set_error(FYG_ERR_NULL_PTR, "null argument");
     const size_t chunks = (plan->batch + plan->chunk - 1) / plan->chunk;
     *launches = plan->strategy == GS_COPY ? 1 : (int)(plan->fwd.size() * chunks);
+    return FYG_OK;
+}
+
+int fyg_plan_describe(const fyg_plan* plan, char* buf, size_t len) {
+    if (!plan || !buf || len == 0) return set_error(FYG_ERR_NULL_PTR, "null argument");
+    static const char* kLoad[] = {"plain", "chirp", "gather"};
+    static const char* kStore[] = {"plain", "chirp", "scatter"};
+    std::string s;
+    for (size_t i = 0; i < plan->fwd.size(); ++i) {
+        const PassDesc& d = plan->fwd[i];
+        char line[256];
+        std::snprintf(line, sizeof(line),
+                      "pass %zu: kernel=%s R=%d C=%d threads=%d smem=%zu Ns=%d Ns_out=%d load=%s%s store=%s%s\n", i,
+                      d.kv == KV_FAST ? "fast" : "generic", d.p.g.R, d.p.g.C, d.threads, d.smem, d.p.Ns, d.p.Ns_out,
+                      kLoad[d.p.load_mode], d.p.Ns > 1 ? "+twiddle" : "", kStore[d.p.store_mode],
+                      d.p.mid ? " mid" : "");
+        s += line;
+    }
+    if (s.size() + 1 > len) return set_error(FYG_ERR_INVALID_ARG, "description buffer too small");
+    std::memcpy(buf, s.c_str(), s.size() + 1);
     return FYG_OK;
 }
 

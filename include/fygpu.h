@@ -56,6 +56,8 @@ extern "C" {
 #define FYG_FLAG_NO_L2_CHUNK 0x4 /* process the whole batch per pass (no L2-resident chunking) */
 #define FYG_FLAG_SMALL_TILES 0x8 /* single-CTA transforms up to ~100 KB of shared memory, stage radix <= 16 */
 #define FYG_FLAG_AUTOTUNED 0x10  /* use the autotuner's cached schedule for this length, if any */
+#define FYG_FLAG_GENERIC_KERNELS 0x20 /* only the generic tile kernel (no register-resident
+                                       * power-of-two kernels); for comparisons */
 
 typedef struct fyg_plan fyg_plan;
 typedef struct fyg_batch fyg_batch;
@@ -109,6 +111,12 @@ int fyg_plan_info(const fyg_plan* plan, size_t* conv_length, int* passes, int* s
 
 /* Kernel launches one fyg_execute of this plan issues (passes x L2 chunks). */
 int fyg_plan_launches(const fyg_plan* plan, int* launches);
+
+/* Plan introspection (no counterpart in the reference): one text line per forward pass with
+ * its kernel ("fast" = register-resident power-of-two kernel, "generic" = shared-memory tile
+ * kernel), tile length R, columns per tile C, threads, shared memory, Ns, Ns_out and the
+ * load/store fusions.  FYG_ERR_INVALID_ARG if `len` is too small. */
+int fyg_plan_describe(const fyg_plan* plan, char* buf, size_t len);
 
 /* Instrumentation (no counterpart in the reference): when enabled, every pass launch of
  * fyg_execute is bracketed by CUDA events on the execution stream and its duration is

@@ -141,3 +141,21 @@ def test_round_trip_and_linearity_large():
     fg.FFT1D_C2C_invoker(n, "complex64", 1).dispatch(False, u, fu)
     torch.cuda.synchronize()
     assert O.rel_l2(fu.cpu().numpy()[0], (a * y[0] + b * y[1]).cpu().numpy()) < 2e-6
+
+
+@pytest.mark.parametrize("n,batch,inverse", [(1 << 20, 9, False), (1 << 20, 9, True), (40009, 64, False),
+                                             (2520, 4096, True)])
+def test_host_pointers_overlapped_chunks(n, batch, inverse):
+    # batches of 8 MB and more from host memory run as copy-in / kernels / copy-out chunks on
+    # three streams; the result must equal the device-resident execution of the same plan
+    x = rand(n, batch, 21)
+    y = np.zeros_like(x)
+    plan = fg.FFT1D_C2C_invoker(n, "complex64", batch)
+    plan.dispatch(inverse, x, y)
+    t = torch.from_numpy(x).cuda()
+    yd = torch.empty_like(t)
+    plan.dispatch(inverse, t, yd)
+    torch.cuda.synchronize()
+    assert np.array_equal(y, yd.cpu().numpy().reshape(y.shape))
+    for b in (0, batch // 2, batch - 1):
+        assert O.rel_l2(y[b], O.fft(x[b], inverse=inverse)) <= 2e-6
