@@ -226,18 +226,21 @@ def run_ours(args, rank: int, world: int):
     for (n, b, *_ ), p in zip(items, plans):
         for i, (tms, nl, bpl) in enumerate(p.profile_read()):
             if nl and (best is None or tms > best[0]):
-                best = (tms, nl, bpl, n, i, len(p.profile_read()))
+                best = (tms, nl, bpl, n, i, len(p.profile_read()), p.describe()[i])
         p.profile(False)
     roof = None
     if best:
-        tms, nl, bpl, n, i, npass = best
+        tms, nl, bpl, n, i, npass, pdesc = best
+        kind = "k_fast" if "kernel=fast" in pdesc else "k_pass"
+        shape = " ".join(w for w in pdesc.split() if w.startswith(("R=", "C=")))
         avg_ms = tms / nl
         achieved = bpl / (avg_ms * 1e-3) / 1e9
         share = tms / (ms_total if ms_total > 0 else 1)
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
                 "frac": round(achieved / hbm_peak, 3), "traffic": read_traffic(n, i),
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else peak_src,
-                "kernel": f"k_pass N={n} pass {i + 1}/{npass}", "bytes_per_launch": int(bpl),
+                "kernel": f"{kind} {shape} (N={n} pass {i + 1}/{npass}{', mid' if ' mid' in pdesc else ''})",
+                "bytes_per_launch": int(bpl),
                 "avg_launch_ms": round(avg_ms, 4), "share_of_step": round(share, 3)}
 
     # end to end through the public API with pinned host buffers (H2D + compute + D2H per step)
