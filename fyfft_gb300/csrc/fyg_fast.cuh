@@ -28,9 +28,10 @@
 
 namespace fyg {
 
-// Shape of a fast tile: R points per column, P registers-points per thread, C columns per tile.
-template <int R_, int P_, int C_> struct FastShape {
-    static constexpr int R = R_, P = P_, C = C_;
+// Shape of a fast tile: R points per column, P registers-points per thread, C columns per tile,
+// TWB: group size of the inter-pass twiddle factorization (fast_twiddle).
+template <int R_, int P_, int C_, int TWB_ = 4> struct FastShape {
+    static constexpr int R = R_, P = P_, C = C_, TWB = TWB_;
     static constexpr int G = R / P;            // threads per column
     static constexpr int T = C * G;            // threads per CTA
     __host__ __device__ static constexpr int pad(int n) { return n >> 5; }
@@ -54,6 +55,13 @@ template <int R_, int P_, int C_> struct FastShape {
     }
     static constexpr size_t smem_bytes() { return (size_t)C * Rp * sizeof(float2); }
 };
+
+// The shapes in use: 256 threads per CTA (two CTAs per SM) up to R = 2048.
+using FastR256 = FastShape<256, 16, 16>;
+using FastR512 = FastShape<512, 32, 16>;
+using FastR1024 = FastShape<1024, 32, 8>;
+using FastR2048 = FastShape<2048, 32, 4>;
+using FastR4096 = FastShape<4096, 32, 4>;
 
 template <class S> __device__ __forceinline__ int fast_addr(int c, int n) { return c * S::Rp + n + S::pad(n); }
 
@@ -105,7 +113,33 @@ __device__ __forceinline__ void fast_stages_from(float2 (&v)[S::P], float2* sm, 
     }
 }
 
-template <class S>
+// Load variants, compiled as separate kernels so that each gets its own register allocation.
+enum FastLoad : int {
+    FL_PLAIN = 0,     // x (conjugated for inverses): first passes
+    FL_TWIDDLE = 1,   // x * w_L^(n k Lr): passes after the first
+    FL_CHIRP = 2,     // Bluestein: x[n] conj(w[n]) for n < N, zero padding above
+    FL_GATHER = 3     // Rader: x[gather[n]], zero where gather < 0; x[0] saved
+};
+
+// Inter-pass twiddles of the thread's points n_i = g + G i, i = B a + b:
+// w^(n_i k Lr) = w^((g + G B a) k Lr) * w^(b G k Lr), i.e. P/B + B - 1 two-level lookups instead
+// of P, and one extra complex product per point (about one more rounding).
+template <int P, int G, int B>
+__device__ __forceinline__ void fast_twiddle(float2 (&v)[P], const PassParams& p, int g, uint32_t kL) {
+    float2 wb[B];
+    wb[0] = make_float2(1.f, 0.f);
+#pragma unroll
+    for (int b = 1; b < B; ++b) wb[b] = tw_two_level(p.tw_hi, p.tw_lo, p.tw_shift, (uint32_t)(b * G) * kL, 0.f);
+#pragma unroll
+    for (int a = 0; a < P / B; ++a) {
+        const uint32_t ea = (uint32_t)(g + G * B * a) * kL;
+        const float2 wa = ea ? tw_two_level(p.tw_hi, p.tw_lo, p.tw_shift, ea, 0.f) : make_float2(1.f, 0.f);
+#pragma unroll
+        for (int b = 0; b < B; ++b) v[a * B + b] = cmul(v[a * B + b], b ? cmul(wa, wb[b]) : wa);
+    }
+}
+
+template <class S, int LD, bool MID>
 __global__ void __launch_bounds__(S::T, (S::T <= 256 ? 2 : 1)) k_fast(const __grid_constant__ PassParams p) {
     extern __shared__ __align__(16) unsigned char smraw[];
     float2* sm = reinterpret_cast<float2*>(smraw);
@@ -119,64 +153,51 @@ __global__ void __launch_bounds__(S::T, (S::T <= 256 ? 2 : 1)) k_fast(const __gr
 
     // ---- load: register i <- x[jj + n Rr], n = g + G i ----
     float2 v[P];
-    {
-        const float2* src = reinterpret_cast<const float2*>(p.in) + ci.in_base + ci.jj;
-        if (p.load_mode == LD_CHIRP) {
-            const float2* chirp = reinterpret_cast<const float2*>(p.chirp);
-            const int64_t nvalid = p.nvalid;
+    const float2* src = reinterpret_cast<const float2*>(p.in) + ci.in_base + ci.jj;
+    if constexpr (LD == FL_CHIRP) {
+        const float2* chirp = reinterpret_cast<const float2*>(p.chirp);
+        const int64_t nvalid = p.nvalid;
 #pragma unroll
-            for (int i = 0; i < P; ++i) {
-                const int gidx = ci.jj + (g + G * i) * Rr;
-                v[i] = make_float2(0.f, 0.f);
-                if (gidx < nvalid) v[i] = ld_data(src + (g + G * i) * Rr);
-            }
+        for (int i = 0; i < P; ++i) {
+            const int gidx = ci.jj + (g + G * i) * Rr;
+            v[i] = make_float2(0.f, 0.f);
+            if (gidx < nvalid) v[i] = ld_data(src + (g + G * i) * Rr);
+        }
+        const float isign = p.conj_in ? -1.f : 1.f;
 #pragma unroll
-            for (int i = 0; i < P; ++i) {
-                const int gidx = ci.jj + (g + G * i) * Rr;
-                if (gidx < nvalid) {
-                    float2 u = v[i];
-                    if (p.conj_in) u.y = -u.y;
-                    v[i] = cmul(u, cconj(__ldg(chirp + gidx)));
-                }
-            }
-        } else if (p.load_mode == LD_GATHER) {
-            // Rader: x[gather[n]] (gather < 0: zero padding); the transform's x[0] is saved
-            const float2* base = reinterpret_cast<const float2*>(p.in) + ci.in_base;
-            const int* gather = p.gather;
+        for (int i = 0; i < P; ++i) {
+            const int gidx = ci.jj + (g + G * i) * Rr;
+            if (gidx < nvalid) v[i] = cmul(make_float2(v[i].x, v[i].y * isign), cconj(__ldg(chirp + gidx)));
+        }
+    } else if constexpr (LD == FL_GATHER) {
+        const float2* base = reinterpret_cast<const float2*>(p.in) + ci.in_base;
+        const int* gather = p.gather;
 #pragma unroll
-            for (int i = 0; i < P; ++i) {
-                const int t = __ldg(gather + ci.jj + (g + G * i) * Rr);
-                v[i] = t >= 0 ? ld_data(base + t) : make_float2(0.f, 0.f);
-            }
-            if (p.conj_in) {
+        for (int i = 0; i < P; ++i) {
+            const int t = __ldg(gather + ci.jj + (g + G * i) * Rr);
+            v[i] = t >= 0 ? ld_data(base + t) : make_float2(0.f, 0.f);
+        }
+        if (p.conj_in) {
 #pragma unroll
-                for (int i = 0; i < P; ++i) v[i].y = -v[i].y;
-            }
-            if (p.x0_from_in && p.x0buf && ci.jj == 0 && g == 0)
-                reinterpret_cast<float2*>(p.x0buf)[ci.b] = ld_data(base);
-        } else {
+            for (int i = 0; i < P; ++i) v[i].y = -v[i].y;
+        }
+        if (p.x0_from_in && p.x0buf && ci.jj == 0 && g == 0)
+            reinterpret_cast<float2*>(p.x0buf)[ci.b] = ld_data(base);
+    } else {
 #pragma unroll
-            for (int i = 0; i < P; ++i) v[i] = ld_data(src + (g + G * i) * Rr);
-            const float isign = p.conj_in ? -1.f : 1.f;
-            if (p.Ns > 1 && ci.k) {
-                const uint32_t kL = (uint32_t)ci.k * (uint32_t)p.Lr;
+        for (int i = 0; i < P; ++i) v[i] = ld_data(src + (g + G * i) * Rr);
+        if (p.conj_in) {
 #pragma unroll
-                for (int i = 0; i < P; ++i) {
-                    const uint32_t e = (uint32_t)(g + G * i) * kL;
-                    float2 u = v[i];
-                    u.y *= isign;
-                    v[i] = e ? cmul(u, tw_two_level(p.tw_hi, p.tw_lo, p.tw_shift, e, 0.f)) : u;
-                }
-            } else {
-#pragma unroll
-                for (int i = 0; i < P; ++i) v[i].y *= isign;
-            }
+            for (int i = 0; i < P; ++i) v[i].y = -v[i].y;
+        }
+        if constexpr (LD == FL_TWIDDLE) {
+            if (ci.k) fast_twiddle<P, G, S::TWB>(v, p, g, (uint32_t)ci.k * (uint32_t)p.Lr);
         }
     }
 
     fast_stages_from<S, 0>(v, sm, c, g, twl);
 
-    if (p.mid) {
+    if constexpr (MID) {
         // forward output point n of this column is global index jj + n Rr of the convolution
         const float2* spec = reinterpret_cast<const float2*>(p.spectrum);
         // Rader: the DC term of the forward convolution FFT (global index 0 = register 0 of

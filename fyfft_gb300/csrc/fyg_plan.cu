@@ -520,7 +520,7 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
         size_t fsm = 0;
         if (pl->dtype == FYG_C32 && cb == 8 && !single &&
             !(pl->flags & (FYG_FLAG_SMALL_TILES | FYG_FLAG_GENERIC_KERNELS)) && fast_shape(R, &fc, &ft, &fsm) &&
-            (L / R) % (uint64_t)fc == 0) {
+            (L / R) % (uint64_t)fc == 0 && !(p.mid && (p.load_mode != LD_PLAIN || p.Ns <= 1))) {
             fill_geom(p.g, R, fc, false, rad);
             d.kv = KV_FAST;
             d.threads = ft;
