@@ -155,19 +155,31 @@ __global__ void __launch_bounds__(S::T, (S::T <= 256 ? 2 : 1)) k_fast(const __gr
     float2 v[P];
     const float2* src = reinterpret_cast<const float2*>(p.in) + ci.in_base + ci.jj;
     if constexpr (LD == FL_CHIRP) {
+        // Unconditional loads at indices clamped into [0, N) and a select for the zero padding:
+        // all loads of the thread are then in flight together (conditional loads were measured
+        // to serialize)
         const float2* chirp = reinterpret_cast<const float2*>(p.chirp);
-        const int64_t nvalid = p.nvalid;
+        const int nlast = (int)p.nvalid - 1;
+        const float2* xb = reinterpret_cast<const float2*>(p.in) + ci.in_base;
 #pragma unroll
-        for (int i = 0; i < P; ++i) {
-            const int gidx = ci.jj + (g + G * i) * Rr;
-            v[i] = make_float2(0.f, 0.f);
-            if (gidx < nvalid) v[i] = ld_data(src + (g + G * i) * Rr);
-        }
+        for (int i = 0; i < P; ++i) v[i] = ld_data(xb + min(ci.jj + (g + G * i) * Rr, nlast));
         const float isign = p.conj_in ? -1.f : 1.f;
+        if (p.tab_tiled) {
+            // conj(chirp) in thread order, zero above N
+            const float2* tab = reinterpret_cast<const float2*>(p.tab_tiled) + (size_t)(ci.jj / C) * (P * S::T) + threadIdx.x;
 #pragma unroll
-        for (int i = 0; i < P; ++i) {
-            const int gidx = ci.jj + (g + G * i) * Rr;
-            if (gidx < nvalid) v[i] = cmul(make_float2(v[i].x, v[i].y * isign), cconj(__ldg(chirp + gidx)));
+            for (int i = 0; i < P; ++i) {
+                const int gidx = ci.jj + (g + G * i) * Rr;
+                const float2 u = cmul(make_float2(v[i].x, v[i].y * isign), __ldg(tab + i * S::T));
+                v[i] = gidx <= nlast ? u : make_float2(0.f, 0.f);
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < P; ++i) {
+                const int gidx = ci.jj + (g + G * i) * Rr;
+                const float2 u = cmul(make_float2(v[i].x, v[i].y * isign), cconj(__ldg(chirp + min(gidx, nlast))));
+                v[i] = gidx <= nlast ? u : make_float2(0.f, 0.f);
+            }
         }
     } else if constexpr (LD == FL_GATHER) {
         const float2* base = reinterpret_cast<const float2*>(p.in) + ci.in_base;
@@ -191,7 +203,14 @@ __global__ void __launch_bounds__(S::T, (S::T <= 256 ? 2 : 1)) k_fast(const __gr
             for (int i = 0; i < P; ++i) v[i].y = -v[i].y;
         }
         if constexpr (LD == FL_TWIDDLE) {
-            if (ci.k) fast_twiddle<P, G, S::TWB>(v, p, g, (uint32_t)ci.k * (uint32_t)p.Lr);
+            if (p.tw_tiled) {
+                const float2* tw = reinterpret_cast<const float2*>(p.tw_tiled) +
+                                   (size_t)((ci.jj / C) & p.tw_tile_mask) * (P * S::T) + threadIdx.x;
+#pragma unroll
+                for (int i = 0; i < P; ++i) v[i] = cmul(v[i], __ldg(tw + i * S::T));
+            } else if (ci.k) {
+                fast_twiddle<P, G, S::TWB>(v, p, g, (uint32_t)ci.k * (uint32_t)p.Lr);
+            }
         }
     }
 
@@ -203,8 +222,14 @@ __global__ void __launch_bounds__(S::T, (S::T <= 256 ? 2 : 1)) k_fast(const __gr
         // Rader: the DC term of the forward convolution FFT (global index 0 = register 0 of
         // thread 0 of column 0)
         if (p.dc_capture && ci.jj == 0 && g == 0) reinterpret_cast<float2*>(p.dcbuf)[ci.b] = v[0];
+        if (p.tab_tiled) {
+            const float2* tab = reinterpret_cast<const float2*>(p.tab_tiled) + (size_t)(ci.jj / C) * (P * S::T) + threadIdx.x;
 #pragma unroll
-        for (int i = 0; i < P; ++i) v[i] = cconj(cmul(v[i], __ldg(spec + ci.jj + (g + G * i) * Rr)));
+            for (int i = 0; i < P; ++i) v[i] = cconj(cmul(v[i], __ldg(tab + i * S::T)));
+        } else {
+#pragma unroll
+            for (int i = 0; i < P; ++i) v[i] = cconj(cmul(v[i], __ldg(spec + ci.jj + (g + G * i) * Rr)));
+        }
         fast_stages_from<S, 0>(v, sm, c, g, twl);
     }
 
@@ -227,16 +252,18 @@ __global__ void __launch_bounds__(S::T, (S::T <= 256 ? 2 : 1)) k_fast(const __gr
         float2* dst = reinterpret_cast<float2*>(p.out) + ci.out_base + ci.out_j;
         const int ns = p.Ns_out;
         if (p.store_mode == ST_CHIRP) {
+            // clamped unconditional table loads, predicated stores (see the chirp load)
             const float2* chirp = reinterpret_cast<const float2*>(p.chirp);
-            const int64_t nvalid = p.nvalid;
+            const int nlast = (int)p.nvalid - 1;
+            const float sy = p.conj_out ? -scale : scale;
+            // the last pass has out_j = jj and Ns_out = Rr: table entry (tile, i, thread)
+            const float2* tab = reinterpret_cast<const float2*>(p.tab_tiled) + (size_t)(ci.jj / C) * (P * S::T) + threadIdx.x;
 #pragma unroll
             for (int i = 0; i < P; ++i) {
                 const int oidx = ci.out_j + (g + G * i) * ns;
-                if (oidx < nvalid) {
-                    float2 u = cscale(cmul(__ldg(chirp + oidx), v[i]), scale);
-                    if (p.conj_out) u.y = -u.y;
-                    dst[(g + G * i) * ns] = u;
-                }
+                const float2 w = p.tab_tiled ? __ldg(tab + i * S::T) : __ldg(chirp + min(oidx, nlast));
+                const float2 u = cmul(w, v[i]);
+                if (oidx <= nlast) dst[(g + G * i) * ns] = make_float2(u.x * scale, u.y * sy);
             }
         } else if (p.store_mode == ST_SCATTER) {
             // Rader: out[scatter[k]] = (x0 + y*scale (conjugated forward)) * scale2, and the DC

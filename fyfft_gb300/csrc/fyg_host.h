@@ -4,6 +4,7 @@
 
 #include <cstdint>
 #include <memory>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -107,6 +108,7 @@ struct fyg_plan {
     std::vector<fyg::PassDesc> fwd, inv;
     // device tables
     std::vector<std::unique_ptr<fyg::DevBuf>> tables;
+    std::map<std::string, const void*> tiled_tables;   // thread-order tables by key (owned by `tables`)
     fyg::DevBuf scratch0, scratch1, x0buf, dcbuf, errword;
     fyg::DevBuf stage_in, stage_out;   // staging for host pointers
     size_t stage_in_bytes = 0;

@@ -3,6 +3,8 @@
 #include "fyg_internal.h"
 #include "fyg_fast.cuh"
 
+#include <algorithm>
+
 namespace fyg {
 
 cudaError_t launch_fast_256(const PassParams& p, unsigned grid, cudaStream_t st);
@@ -29,6 +31,58 @@ bool fast_shape(int R, int* C, int* threads, size_t* smem) {
         case 4096: return shape_of<FastR4096>(C, threads, smem);
         default: return false;
     }
+}
+
+int fast_points(int R) {
+    switch (R) {
+        case 256: return FastR256::P;
+        case 512: return FastR512::P;
+        case 1024: return FastR1024::P;
+        case 2048: return FastR2048::P;
+        case 4096: return FastR4096::P;
+        default: return 0;
+    }
+}
+
+// Tables in the fast kernels' thread order: entry ((t P + i) T + tid) belongs to thread
+// tid = g C + c of tile t, register i, i.e. point n = g + G i of column jj = t C + c.
+//   kind 0: inter-pass twiddle exp(-2 pi i n jj Lr / L), from the FP64 sincospi of the exactly
+//           reduced exponent, rounded once
+//   kind 1: src[jj + n Rr] (conjugated if conj), zero at and above nvalid
+__global__ void k_fast_table(float2* out, uint64_t total, int P, int C, int T, int kind, uint64_t Lr, uint64_t L,
+                             uint64_t Rr, const float2* src, int64_t nvalid, int conj) {
+    const int G = T / C;
+    for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (uint64_t)gridDim.x * blockDim.x) {
+        const int tid = (int)(idx % T);
+        const uint64_t q = idx / T;
+        const int i = (int)(q % P);
+        const uint64_t t = q / P;
+        const int c = tid % C, g = tid / C;
+        const uint64_t n = (uint64_t)g + (uint64_t)G * i, jj = t * C + c;
+        float2 w;
+        if (kind == 0) {
+            const uint64_t e = (n * jj % L) * Lr % L;
+            double sn, cs;
+            sincospi(2.0 * (double)e / (double)L, &sn, &cs);
+            w = make_float2((float)cs, (float)-sn);
+        } else {
+            const uint64_t gi = jj + n * Rr;
+            w = (int64_t)gi < nvalid ? src[gi] : make_float2(0.f, 0.f);
+            if (conj) w.y = -w.y;
+        }
+        out[idx] = w;
+    }
+}
+
+cudaError_t launch_fast_table(float2* out, uint64_t total, int R, int kind, uint64_t Lr, uint64_t L, uint64_t Rr,
+                              const float2* src, int64_t nvalid, int conj, cudaStream_t st) {
+    int C = 0, T = 0;
+    size_t smem = 0;
+    if (!fast_shape(R, &C, &T, &smem)) return cudaErrorInvalidValue;
+    const unsigned blocks = (unsigned)std::min<uint64_t>((total + 255) / 256, 1u << 16);
+    k_fast_table<<<blocks, 256, 0, st>>>(out, total, fast_points(R), C, T, kind, Lr, L, Rr, src, nvalid, conj);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_fast(const PassParams& p, unsigned grid, cudaStream_t st) {

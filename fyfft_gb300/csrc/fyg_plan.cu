@@ -525,6 +525,34 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
             d.kv = KV_FAST;
             d.threads = ft;
             d.smem = fsm;
+            // thread-order tables (shared by the forward and inverse pipelines)
+            auto tiled = [&](const std::string& key, uint64_t total, int kind, const void* src, int64_t nvalid,
+                             int conj, const void** outp) -> int {
+                auto it = pl->tiled_tables.find(key);
+                if (it != pl->tiled_tables.end()) { *outp = it->second; return FYG_OK; }
+                auto buf = std::make_unique<DevBuf>();
+                int rc = buf->alloc(total * sizeof(float2));
+                if (rc) return rc;
+                cudaError_t e = launch_fast_table(static_cast<float2*>(buf->ptr), total, R, kind, (uint64_t)p.Lr, L,
+                                                  (uint64_t)p.Rr, static_cast<const float2*>(src), nvalid, conj, 0);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+                if (e != cudaSuccess) return cuda_error(e, "thread-order table");
+                *outp = buf->ptr;
+                pl->tiled_tables[key] = buf->ptr;
+                pl->tables.push_back(std::move(buf));
+                return FYG_OK;
+            };
+            const std::string sh = std::to_string(R) + ":" + std::to_string(Ns) + ":" + std::to_string(L);
+            int rc = FYG_OK;
+            if (p.Ns > 1 && p.load_mode == LD_PLAIN) {
+                rc = tiled("tw:" + sh, Ns * (uint64_t)R, 0, nullptr, 0, 0, &p.tw_tiled);
+                p.tw_tile_mask = (int)(Ns / (uint64_t)fc) - 1;
+            }
+            if (!rc && p.mid) rc = tiled("spec:" + sh, L, 1, ct.spectrum, (int64_t)L, 0, &p.tab_tiled);
+            else if (!rc && p.load_mode == LD_CHIRP) rc = tiled("chin:" + sh, L, 1, ct.chirp, (int64_t)n, 1, &p.tab_tiled);
+            else if (!rc && p.store_mode == ST_CHIRP && p.Ns_out == p.Rr)
+                rc = tiled("chout:" + sh, L, 1, ct.chirp, (int64_t)n, 0, &p.tab_tiled);
+            if (rc) return rc;
         }
         if (d.smem > kSmemLimit)
             return set_error(FYG_ERR_UNSUPPORTED, "tile of " + std::to_string(R) + "x" + std::to_string(C) +
