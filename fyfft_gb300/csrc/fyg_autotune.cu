@@ -4,7 +4,9 @@
 //   single-pass lengths   transforms per CTA (C), i.e. threads per transform = threads / C
 //   multi-pass lengths    a cap on the pass radix (more, smaller passes or fewer, larger ones)
 //   Rader / Bluestein     the convolution length (7-smooth lengths up to 8% above the minimum,
-//                         and for Bluestein the power of two) and a cap on its pass radix
+//                         and for Bluestein the power of two), a cap on its pass radix and the
+//                         pass order (which radix the fused mid pass takes)
+// FYG_AUTOTUNE_VERBOSE=1 lists every candidate's time on stderr.
 // Every candidate plan runs a forward batch on the current device (CUDA events, best of three
 // after a warm-up); the fastest is written to the cache under "c32:<n>" / "c64:<n>" together
 // with the device signature (name, SM count, compute capability, driver).  A cache written
@@ -71,14 +73,16 @@ void load(const std::string& path) {
         }
         char key[64];
         unsigned long long r = 0, m = 0;
-        int c = 0;
+        int c = 0, o = 0;
         double ms = 0;
-        if (std::sscanf(line.c_str(), " \"%63[^\"]\": {\"max_pass_radix\": %llu, \"conv_length\": %llu, \"cols\": %d, \"ms\": %lf",
-                        key, &r, &m, &c, &ms) == 5) {
+        if (std::sscanf(line.c_str(),
+                        " \"%63[^\"]\": {\"max_pass_radix\": %llu, \"conv_length\": %llu, \"cols\": %d, \"order\": %d, \"ms\": %lf",
+                        key, &r, &m, &c, &o, &ms) == 6) {
             TuneChoice t;
             t.max_pass_radix = r;
             t.conv_length = m;
             t.cols = c;
+            t.order = o;
             t.ms = ms;
             g_cache.entries[key] = t;
         }
@@ -95,9 +99,10 @@ int save() {
     size_t i = 0;
     for (auto& kv : g_cache.entries) {
         char buf[256];
-        std::snprintf(buf, sizeof(buf), "    \"%s\": {\"max_pass_radix\": %llu, \"conv_length\": %llu, \"cols\": %d, \"ms\": %.6f}%s\n",
+        std::snprintf(buf, sizeof(buf),
+                      "    \"%s\": {\"max_pass_radix\": %llu, \"conv_length\": %llu, \"cols\": %d, \"order\": %d, \"ms\": %.6f}%s\n",
                       kv.first.c_str(), (unsigned long long)kv.second.max_pass_radix,
-                      (unsigned long long)kv.second.conv_length, kv.second.cols, kv.second.ms,
+                      (unsigned long long)kv.second.conv_length, kv.second.cols, kv.second.order, kv.second.ms,
                       ++i < g_cache.entries.size() ? "," : "");
         f << buf;
     }
@@ -129,11 +134,12 @@ std::vector<TuneChoice> candidates(size_t n, int dtype, size_t batch) {
     const int cb = dtype == FYG_C32 ? 8 : 16;
     std::vector<TuneChoice> out;
     out.push_back(TuneChoice());
-    auto add = [&](uint64_t r, uint64_t m, int c) {
+    auto add = [&](uint64_t r, uint64_t m, int c, int o = 0) {
         TuneChoice t;
         t.max_pass_radix = r;
         t.conv_length = m;
         t.cols = c;
+        t.order = o;
         out.push_back(t);
     };
     if (smooth(n, 13)) {
@@ -142,6 +148,7 @@ std::vector<TuneChoice> candidates(size_t n, int dtype, size_t batch) {
                 if ((size_t)c <= batch && (uint64_t)c * n <= 16384) add(0, 0, c);
         } else {
             for (uint64_t r : {2048ull, 1024ull, 512ull, 256ull, 128ull}) add(r, 0, 0);
+            add(0, 0, 0, 1);
         }
         return out;
     }
@@ -155,7 +162,8 @@ std::vector<TuneChoice> candidates(size_t n, int dtype, size_t batch) {
         if (std::find(ms.begin(), ms.end(), m2) == ms.end()) ms.push_back(m2);
     }
     for (uint64_t m : ms)
-        for (uint64_t r : {0ull, 256ull}) add(r, m, 0);
+        for (uint64_t r : {0ull, 256ull})
+            for (int o : {0, 1}) add(r, m, 0, o);
     return out;
 }
 
@@ -192,9 +200,11 @@ extern "C" int fyg_autotune(size_t n, int dtype, size_t batch, const char* cache
     cudaEventCreate(&e1);
     TuneChoice best;
     bool have = false;
+    const bool verbose = std::getenv("FYG_AUTOTUNE_VERBOSE") != nullptr;
     for (const TuneChoice& c : candidates(n, dtype, batch)) {
         fyg_plan* pl = nullptr;
-        if (plan_create_opts(n, dtype, batch, 0, c.max_pass_radix, c.conv_length, c.cols, &pl) != FYG_OK) continue;
+        if (plan_create_opts(n, dtype, batch, 0, c.max_pass_radix, c.conv_length, c.cols, c.order, &pl) != FYG_OK)
+            continue;
         double t = 1e30;
         bool ok = fyg_execute(pl, in.ptr, out.ptr, FYG_FORWARD, nullptr) == FYG_OK;
         for (int rep = 0; rep < 3 && ok; ++rep) {
@@ -207,6 +217,10 @@ extern "C" int fyg_autotune(size_t n, int dtype, size_t batch, const char* cache
             t = std::min(t, (double)ms);
         }
         fyg_plan_destroy(pl);
+        if (verbose)
+            std::fprintf(stderr, "fyg_autotune n=%zu max_pass_radix=%llu conv_length=%llu cols=%d order=%d: %s %.4f ms\n", n,
+                         (unsigned long long)c.max_pass_radix, (unsigned long long)c.conv_length, c.cols, c.order,
+                         ok ? "ok" : "failed", ok ? t : 0.0);
         if (ok && (!have || t < best.ms)) {
             best = c;
             best.ms = t;

@@ -39,11 +39,12 @@ std::vector<unsigned char> host_local_table(int R, int cb);
 struct TuneChoice {
     uint64_t max_pass_radix = 0, conv_length = 0;
     int cols = 0;
+    int order = 0;       // 1: reversed pass order (the fused mid pass takes the other radix)
     double ms = 0;
 };
 bool tune_lookup(size_t n, int dtype, TuneChoice* out);
 int plan_create_opts(size_t n, int dtype, size_t batch, int flags, uint64_t max_pass_radix, uint64_t conv_length,
-                     int cols, fyg_plan** out);
+                     int cols, int order, fyg_plan** out);
 void host_two_level(uint64_t L, int cb, std::vector<unsigned char>& hi, std::vector<unsigned char>& lo, int* shift);
 
 // GPU-side strategy of a plan (what actually runs).

@@ -258,6 +258,7 @@ bool tile_fits(int cb, int R, int C, bool colmajor) {
 // plan's creation.
 static thread_local uint64_t t_max_pass_r = 0;
 static thread_local uint64_t t_conv_len = 0;
+static thread_local int t_order = 0;  // 1: reversed pass order
 static thread_local int t_cols = 0;   // single-pass: transforms per CTA (threads per transform = T/C)
 
 bool split_passes(uint64_t L, int cb, bool conv, std::vector<int>& out) {
@@ -632,6 +633,11 @@ static int make_plan(fyg_plan* pl) {
             ps.prad = {(int)ps.L};
         } else if (!split_passes(ps.L, cb, conv, ps.prad)) {
             return set_error(FYG_ERR_UNSUPPORTED, "no pass decomposition for length " + std::to_string(ps.L));
+        } else if (t_order) {
+            std::reverse(ps.prad.begin(), ps.prad.end());
+            for (int R : ps.prad)
+                if (!tile_fits(cb, R, multi_C(cb, R), false) || (conv && R == ps.prad.back() && !multi_C(cb, R)))
+                    return set_error(FYG_ERR_UNSUPPORTED, "reversed pass order does not fit shared memory");
         }
     }
     const int P = (int)ps.prad.size();
@@ -961,12 +967,15 @@ static int execute_dir(fyg_plan* pl, const void* in, void* out, bool inverse, do
 static int gpu_fft_f64(size_t n, const std::vector<double2>& h, std::vector<double2>& H) {
     fyg_plan* sub = nullptr;
     const uint64_t keep_r = t_max_pass_r, keep_m = t_conv_len;
+    const int keep_order = t_order;
+    t_order = 0;
     const int keep_cap = t_radix_cap, keep_cols = t_cols;
     t_max_pass_r = t_conv_len = 0;
     t_radix_cap = t_cols = 0;
     int rc = fyg_plan_create(n, FYG_C64, 1, 0, &sub);
     t_max_pass_r = keep_r;
     t_conv_len = keep_m;
+    t_order = keep_order;
     t_radix_cap = keep_cap;
     t_cols = keep_cols;
     if (rc) return rc;
@@ -1001,14 +1010,16 @@ fyg_plan::~fyg_plan() {
 namespace fyg {
 // plan creation with explicit schedule options (0 = default); used by the autotuner
 int plan_create_opts(size_t n, int dtype, size_t batch, int flags, uint64_t max_pass_radix, uint64_t conv_length,
-                     int cols, fyg_plan** out) {
+                     int cols, int order, fyg_plan** out) {
     t_max_pass_r = max_pass_radix;
     t_conv_len = conv_length;
     t_cols = cols;
+    t_order = order;
     const int rc = fyg_plan_create(n, dtype, batch, flags & ~FYG_FLAG_AUTOTUNED, out);
     t_max_pass_r = 0;
     t_conv_len = 0;
     t_cols = 0;
+    t_order = 0;
     return rc;
 }
 }  // namespace fyg
@@ -1017,7 +1028,7 @@ extern "C" {
 
 int fyg_plan_create_ex(size_t n, int dtype, size_t batch, int flags, size_t max_pass_radix, size_t conv_length,
                        fyg_plan** out) {
-    return plan_create_opts(n, dtype, batch, flags & ~FYG_FLAG_AUTOTUNED, max_pass_radix, conv_length, 0, out);
+    return plan_create_opts(n, dtype, batch, flags & ~FYG_FLAG_AUTOTUNED, max_pass_radix, conv_length, 0, 0, out);
 }
 
 
@@ -1025,8 +1036,8 @@ int fyg_plan_create(size_t n, int dtype, size_t batch, int flags, fyg_plan** out
     clear_error();
     if (flags & FYG_FLAG_AUTOTUNED) {
         TuneChoice tc;
-        if (tune_lookup(n, dtype, &tc)) return plan_create_opts(n, dtype, batch, flags, tc.max_pass_radix,
-                                                                tc.conv_length, tc.cols, out);
+        if (tune_lookup(n, dtype, &tc))
+            return plan_create_opts(n, dtype, batch, flags, tc.max_pass_radix, tc.conv_length, tc.cols, tc.order, out);
         flags &= ~FYG_FLAG_AUTOTUNED;
     }
     if (!out) return set_error(FYG_ERR_NULL_PTR, "out is null");
