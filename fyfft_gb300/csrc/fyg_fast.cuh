@@ -28,16 +28,18 @@
 
 namespace fyg {
 
-// Shape of a fast tile: R points per column, P registers-points per thread, C columns per tile,
-// TWB: group size of the inter-pass twiddle factorization (fast_twiddle).
+// Shape of a fast tile: R points per column, P registers-points per thread (every stage radix
+// divides P), C columns per tile, TWB: group size of the inter-pass twiddle factorization
+// (fast_twiddle, used when no thread-order table was built).
 template <int R_, int P_, int C_, int TWB_ = 4> struct FastShape {
     static constexpr int R = R_, P = P_, C = C_, TWB = TWB_;
+    static_assert(P % TWB == 0, "twiddle groups must tile the registers");
     static constexpr int G = R / P;            // threads per column
     static constexpr int T = C * G;            // threads per CTA
     __host__ __device__ static constexpr int pad(int n) { return n >> 5; }
-    // pitch of a column: >= R + R/32 and = 16/C (mod 16) (8-byte words), so the C columns of a
-    // half-warp start in different banks
-    static constexpr int Rp = ((R + (R >> 5) + 15) & ~15) + 16 / C;
+    // pitch of a column: >= R + R/32 and = 16/C (mod 16) (8-byte words; 1 for C >= 16), so
+    // the columns met by a half-warp start in different banks
+    static constexpr int Rp = ((R + (R >> 5) + 15) & ~15) + (C >= 16 ? 1 : 16 / C);
     __host__ __device__ static constexpr int nst() {
         int s = 0;
         for (int rem = R; rem > 1; rem /= (rem < P ? rem : P)) ++s;
@@ -56,12 +58,15 @@ template <int R_, int P_, int C_, int TWB_ = 4> struct FastShape {
     static constexpr size_t smem_bytes() { return (size_t)C * Rp * sizeof(float2); }
 };
 
-// The shapes in use: 256 threads per CTA (two CTAs per SM) up to R = 2048.
+// The shapes in use: 256 threads per CTA (two CTAs per SM) up to R = 2048; 243 = 27 * 9 and
+// 343 = 7 * 7 * 7 for powers of three and seven (C divides their column counts 3^k / 7^k).
 using FastR256 = FastShape<256, 16, 16>;
 using FastR512 = FastShape<512, 32, 16>;
 using FastR1024 = FastShape<1024, 32, 8>;
 using FastR2048 = FastShape<2048, 32, 4>;
 using FastR4096 = FastShape<4096, 32, 4>;
+using FastR243 = FastShape<243, 27, 27, 3>;
+using FastR343 = FastShape<343, 7, 7, 7>;
 
 template <class S> __device__ __forceinline__ int fast_addr(int c, int n) { return c * S::Rp + n + S::pad(n); }
 
@@ -79,7 +84,7 @@ __device__ __forceinline__ void fast_stage(float2 (&v)[S::P], float2* sm, int c,
 #pragma unroll
         for (int m = 0; m < r; ++m) x[m] = v[b + m * nb];
         const int j = g + S::G * b;
-        const int k = j & (ns - 1);
+        const int k = j % ns;
         if constexpr (ST > 0) {
             if (k) {
                 const int t = k * twm;
@@ -140,11 +145,11 @@ __device__ __forceinline__ void fast_twiddle(float2 (&v)[P], const PassParams& p
 }
 
 template <class S, int LD, bool MID>
-__global__ void __launch_bounds__(S::T, (S::T <= 256 ? 2 : 1)) k_fast(const __grid_constant__ PassParams p) {
+__global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1)) k_fast(const __grid_constant__ PassParams p) {
     extern __shared__ __align__(16) unsigned char smraw[];
     float2* sm = reinterpret_cast<float2*>(smraw);
     constexpr int P = S::P, G = S::G, C = S::C, R = S::R;
-    const int c = threadIdx.x & (C - 1);
+    const int c = threadIdx.x % C;
     const int g = threadIdx.x / C;
     // all C columns of a tile belong to one transform (Rr is a multiple of C)
     const Col<float> ci = make_col<float, float>(p, (int64_t)blockIdx.x * C + c);
@@ -205,7 +210,7 @@ __global__ void __launch_bounds__(S::T, (S::T <= 256 ? 2 : 1)) k_fast(const __gr
         if constexpr (LD == FL_TWIDDLE) {
             if (p.tw_tiled) {
                 const float2* tw = reinterpret_cast<const float2*>(p.tw_tiled) +
-                                   (size_t)((ci.jj / C) & p.tw_tile_mask) * (P * S::T) + threadIdx.x;
+                                   (size_t)((ci.jj / C) % p.tw_tile_period) * (P * S::T) + threadIdx.x;
 #pragma unroll
                 for (int i = 0; i < P; ++i) v[i] = cmul(v[i], __ldg(tw + i * S::T));
             } else if (ci.k) {
@@ -245,7 +250,7 @@ __global__ void __launch_bounds__(S::T, (S::T <= 256 ? 2 : 1)) k_fast(const __gr
         float2* dst = reinterpret_cast<float2*>(p.out) + ci.out_base + jj0 * R;
 #pragma unroll 4
         for (int e = threadIdx.x; e < C * R; e += S::T) {
-            const float2 u = sm[fast_addr<S>(e / R, e & (R - 1))];
+            const float2 u = sm[fast_addr<S>(e / R, e % R)];
             dst[e] = make_float2(u.x * scale, u.y * sy);
         }
     } else {

@@ -12,6 +12,8 @@ cudaError_t launch_fast_512(const PassParams& p, unsigned grid, cudaStream_t st)
 cudaError_t launch_fast_1024(const PassParams& p, unsigned grid, cudaStream_t st);
 cudaError_t launch_fast_2048(const PassParams& p, unsigned grid, cudaStream_t st);
 cudaError_t launch_fast_4096(const PassParams& p, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_243(const PassParams& p, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_343(const PassParams& p, unsigned grid, cudaStream_t st);
 
 namespace {
 template <class S> bool shape_of(int* C, int* threads, size_t* smem) {
@@ -29,6 +31,8 @@ bool fast_shape(int R, int* C, int* threads, size_t* smem) {
         case 1024: return shape_of<FastR1024>(C, threads, smem);
         case 2048: return shape_of<FastR2048>(C, threads, smem);
         case 4096: return shape_of<FastR4096>(C, threads, smem);
+        case 243: return shape_of<FastR243>(C, threads, smem);
+        case 343: return shape_of<FastR343>(C, threads, smem);
         default: return false;
     }
 }
@@ -40,6 +44,8 @@ int fast_points(int R) {
         case 1024: return FastR1024::P;
         case 2048: return FastR2048::P;
         case 4096: return FastR4096::P;
+        case 243: return FastR243::P;
+        case 343: return FastR343::P;
         default: return 0;
     }
 }
@@ -92,6 +98,8 @@ cudaError_t launch_fast(const PassParams& p, unsigned grid, cudaStream_t st) {
         case 1024: return launch_fast_1024(p, grid, st);
         case 2048: return launch_fast_2048(p, grid, st);
         case 4096: return launch_fast_4096(p, grid, st);
+        case 243: return launch_fast_243(p, grid, st);
+        case 343: return launch_fast_343(p, grid, st);
         default: return cudaErrorInvalidValue;
     }
 }

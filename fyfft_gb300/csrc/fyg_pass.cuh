@@ -95,11 +95,11 @@ struct alignas(16) PassParams {
     // register-resident kernels (fyg_fast.cuh): tables laid out in the kernel's thread order,
     // entry ((t P + i) T + tid) for tile t of a transform, register i of thread tid; null when
     // not built.  tw_tiled: inter-pass twiddles of the first Ns/C tiles (the pattern repeats
-    // with period Ns/C tiles, tw_tile_mask = Ns/C - 1); tab_tiled: the spectrum (mid pass), the
+    // with period tw_tile_period = Ns/C tiles); tab_tiled: the spectrum (mid pass), the
     // conjugated zero-padded chirp (chirp load) or the chirp (chirp store)
     const void* tw_tiled;
     const void* tab_tiled;
-    int tw_tile_mask;
+    int tw_tile_period;
 };
 
 __device__ __forceinline__ int64_t transform_base(const int64_t* offs, const int* ids, int64_t b, int64_t dist) {

@@ -515,13 +515,15 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
         d.threads = threads_for(R, C, kMaxThreads);
         d.kv = pick_variant(cb, (int)d.in_elem_bytes, (int)d.out_elem_bytes, cls);
         d.smem = smem_for(cb, R, C, single);
-        // register-resident kernel for power-of-two tiles of FP32 passes (not for the tiles of
-        // uneven batches, which run inside the generic persistent kernel)
+        // register-resident kernel for the tile lengths it is compiled for (FP32; not for the
+        // tiles of uneven batches, which run inside the generic persistent kernel); the
+        // inter-pass twiddle table needs C | Ns
         int fc = 0, ft = 0;
         size_t fsm = 0;
         if (pl->dtype == FYG_C32 && cb == 8 && !single &&
             !(pl->flags & (FYG_FLAG_SMALL_TILES | FYG_FLAG_GENERIC_KERNELS)) && fast_shape(R, &fc, &ft, &fsm) &&
-            (L / R) % (uint64_t)fc == 0 && !(p.mid && (p.load_mode != LD_PLAIN || p.Ns <= 1))) {
+            (L / R) % (uint64_t)fc == 0 && !(p.mid && (p.load_mode != LD_PLAIN || p.Ns <= 1)) &&
+            (p.Ns <= 1 || p.Ns % fc == 0)) {
             fill_geom(p.g, R, fc, false, rad);
             d.kv = KV_FAST;
             d.threads = ft;
@@ -547,7 +549,7 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
             int rc = FYG_OK;
             if (p.Ns > 1 && p.load_mode == LD_PLAIN) {
                 rc = tiled("tw:" + sh, Ns * (uint64_t)R, 0, nullptr, 0, 0, &p.tw_tiled);
-                p.tw_tile_mask = (int)(Ns / (uint64_t)fc) - 1;
+                p.tw_tile_period = (int)(Ns / (uint64_t)fc);
             }
             if (!rc && p.mid) rc = tiled("spec:" + sh, L, 1, ct.spectrum, (int64_t)L, 0, &p.tab_tiled);
             else if (!rc && p.load_mode == LD_CHIRP) rc = tiled("chin:" + sh, L, 1, ct.chirp, (int64_t)n, 1, &p.tab_tiled);

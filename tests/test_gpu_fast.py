@@ -88,3 +88,22 @@ def test_round_trip_and_adjoint_on_fast_plan():
     # adjoint of the unnormalized DFT = N * inverse
     ref = O.fft(x.reshape(batch, n)[1], inverse=True) * n
     assert O.rel_l2(a.cpu().numpy().reshape(batch, n)[1], ref) <= 4 * np.log2(n) * EPS32
+
+
+# tile lengths 243 = 27 * 9 and 343 = 7 * 7 * 7 (columns per tile 27 and 7, not powers of two)
+@pytest.mark.parametrize("n,batch,fast", [(59049, 8, 2), (117649, 4, 2), (16807, 16, 1), (177147, 2, 1)])
+@pytest.mark.parametrize("inverse", [False, True])
+def test_power_of_three_and_seven_passes(n, batch, fast, inverse):
+    p, x, y = run(n, batch, inverse)
+    assert kernels(p).count("fast") >= fast, p.describe()
+    for b in (0, batch - 1):
+        assert O.rel_l2(y[b], O.fft(x[b], inverse=inverse)) <= 4 * np.log2(n) * EPS32
+
+
+@pytest.mark.parametrize("inverse", [False, True])
+def test_bluestein_on_243_tiles(inverse):
+    n = 29000                      # 2^3 5^3 29: Bluestein, convolution 59049 = 243 * 243
+    p, x, y = run(n, 3, inverse, conv_length=59049)
+    assert kernels(p) == ["fast"] * 3, p.describe()
+    for b in range(3):
+        assert O.rel_l2(y[b], O.fft(x[b], inverse=inverse)) <= 2e-6
