@@ -284,13 +284,13 @@ def run_ours(args, rank: int, world: int):
         "per_size": per_size,
     }
     if not args.no_uneven:
-        out["batched_vs_plain"] = uneven_batch(dev, stream)
+        out["batched_vs_plain"] = uneven_batch(dev, stream, no_autotune=args.no_autotune)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(items, args, check=(plans, yout))
     return out
 
 
-def uneven_batch(dev: int, stream, reps: int = 10):
+def uneven_batch(dev: int, stream, reps: int = 10, no_autotune: bool = False):
     """The mixed-length batch (4096 lengths in [16, 65536], 7-smooth / prime / other, seed 2):
     one persistent launch (CUDA graph) against one launch sequence per transform."""
     import torch
@@ -298,14 +298,21 @@ def uneven_batch(dev: int, stream, reps: int = 10):
     from fyfft_gb300.workloads import uneven_lengths
     lengths = uneven_lengths(4096, 2)
     t0 = time.perf_counter()
-    b = fg.UnevenBatch(lengths)
-    create_s = time.perf_counter() - t0
+    tuned = None
+    if not no_autotune:
+        # option sets of the persistent launch timed on this device, cached (FYG_AUTOTUNE_CACHE)
+        fg.autotune_batch(lengths, cache_path=os.environ.get("FYG_AUTOTUNE_CACHE"))
+        tuned = round(time.perf_counter() - t0, 2)
+    t1 = time.perf_counter()
+    b = fg.UnevenBatch(lengths, flags=0 if no_autotune else fg.FYG_FLAG_AUTOTUNED)
+    create_s = time.perf_counter() - t1
     x = torch.from_numpy(fg.fill_random(2, sum(lengths), np.complex64, "uniform")).to(f"cuda:{dev}")
     y = torch.empty_like(x)
     fl = sum(flops(n) for n in lengths)
     res = {"workload": "4096 complex<float> transforms, lengths log-uniform in [16, 65536] "
                        "(0.70 7-smooth / 0.15 prime / 0.15 other), uniform[-1,1] seed 2, packed back to back",
-           "points": int(sum(lengths)), "distinct_lengths": len(set(lengths)), "create_s": round(create_s, 2)}
+           "points": int(sum(lengths)), "distinct_lengths": len(set(lengths)), "create_s": round(create_s, 2),
+           "autotune_s": tuned}
     for name, f in (("batched", lambda: b.execute(x, y, stream=stream)),
                     ("plain", lambda: b.execute_plain(x, y, stream=stream))):
         for _ in range(3):

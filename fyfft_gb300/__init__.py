@@ -35,7 +35,7 @@ FYG_FLAG_SMALL_TILES, FYG_FLAG_AUTOTUNED, FYG_FLAG_GENERIC_KERNELS = 8, 16, 32
 EXPORTED_SYMBOLS = (
     "fyg_plan_create", "fyg_plan_create_ex", "fyg_autotune", "fyg_plan_destroy", "fyg_execute", "fyg_execute_adjoint", "fyg_strategy",
     "fyg_gpu_strategy", "fyg_plan_info", "fyg_plan_launches", "fyg_plan_describe", "fyg_plan_profile",
-    "fyg_plan_profile_read", "fyg_batch_create", "fyg_batch_destroy",
+    "fyg_plan_profile_read", "fyg_batch_create", "fyg_batch_autotune", "fyg_batch_destroy",
     "fyg_batch_execute", "fyg_batch_execute_plain", "fyg_batch_status", "fyg_batch_inject_stall",
     "fyg_execute_noalloc", "fyg_last_error_string",
     "fyg_fill_random",
@@ -84,6 +84,7 @@ def lib() -> ctypes.CDLL:
         L.fyg_plan_profile_read.argtypes = [vp, ctypes.POINTER(d), ctypes.POINTER(ctypes.c_int64),
                                             ctypes.POINTER(ctypes.c_int64), i, ctypes.POINTER(i)]
         L.fyg_batch_create.argtypes = [ctypes.POINTER(sz), sz, i, i, ctypes.POINTER(vp)]
+        L.fyg_batch_autotune.argtypes = [ctypes.POINTER(sz), sz, i, ctypes.c_char_p, ctypes.POINTER(d)]
         L.fyg_batch_destroy.argtypes = [vp]
         L.fyg_batch_execute.argtypes = [vp, vp, vp, vp, i, vp]
         L.fyg_batch_execute_plain.argtypes = [vp, vp, vp, i, vp]
@@ -107,6 +108,18 @@ def autotune(length: int, dtype="complex64", batch: int = 1, cache_path: str | N
     ms = ctypes.c_double()
     path = cache_path.encode() if cache_path else None
     check(lib().fyg_autotune(int(length), code, int(batch), path, ctypes.byref(ms)))
+    return ms.value
+
+
+def autotune_batch(lengths, dtype="complex64", cache_path: str | None = None) -> float:
+    """Time the uneven-batch option sets for this length sequence and cache the fastest; create
+    the batch with flags=FYG_FLAG_AUTOTUNED to use it.  Returns the winner's milliseconds."""
+    lens = [int(n) for n in lengths]
+    arr = (ctypes.c_size_t * len(lens))(*lens)
+    code = FYG_C32 if str(dtype).endswith("complex64") else FYG_C64
+    ms = ctypes.c_double()
+    path = cache_path.encode() if cache_path else None
+    check(lib().fyg_batch_autotune(arr, len(lens), code, path, ctypes.byref(ms)))
     return ms.value
 
 

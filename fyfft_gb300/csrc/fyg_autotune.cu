@@ -169,14 +169,29 @@ std::vector<TuneChoice> candidates(size_t n, int dtype, size_t batch) {
 
 }  // namespace
 
-bool tune_lookup(size_t n, int dtype, TuneChoice* out) {
+bool tune_lookup_key(const std::string& key, TuneChoice* out) {
     std::lock_guard<std::mutex> lk(g_mu);
     if (!g_cache.loaded) load(default_path());
     if (g_cache.device != device_signature()) return false;
-    auto it = g_cache.entries.find(key_of(n, dtype));
+    auto it = g_cache.entries.find(key);
     if (it == g_cache.entries.end()) return false;
     *out = it->second;
     return true;
+}
+
+bool tune_lookup(size_t n, int dtype, TuneChoice* out) { return tune_lookup_key(key_of(n, dtype), out); }
+
+int tune_store_key(const std::string& key, const TuneChoice& choice, const char* cache_path) {
+    const std::string path = cache_path ? cache_path : default_path();
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_cache.loaded || g_cache.path != path) load(path);
+    const std::string dev = device_signature();
+    if (g_cache.device != dev) {
+        g_cache.entries.clear();
+        g_cache.device = dev;
+    }
+    g_cache.entries[key] = choice;
+    return save();
 }
 
 }  // namespace fyg
@@ -231,14 +246,6 @@ extern "C" int fyg_autotune(size_t n, int dtype, size_t batch, const char* cache
     cudaEventDestroy(e1);
     clear_error();
     if (!have) return set_error(FYG_ERR_UNSUPPORTED, "autotune: no candidate plan ran");
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_cache.loaded || g_cache.path != path) load(path);
-    const std::string dev = device_signature();
-    if (g_cache.device != dev) {
-        g_cache.entries.clear();
-        g_cache.device = dev;
-    }
-    g_cache.entries[key_of(n, dtype)] = best;
     if (best_ms) *best_ms = best.ms;
-    return save();
+    return tune_store_key(key_of(n, dtype), best, path.c_str());
 }

@@ -13,10 +13,13 @@
 // expiry the kernel sets an error word and an abort flag, every CTA returns, and
 // fyg_batch_status reports FYG_ERR_TIMEOUT.
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <map>
 #include <memory>
 #include <mutex>
 #include <numeric>
+#include <string>
 #include <vector>
 
 #include "fyg_host.h"
@@ -275,6 +278,33 @@ int launch_persistent(fyg_batch* b, const void* in, void* out, const int64_t* of
 
 }  // namespace
 
+namespace {
+
+// Autotune cache key of a batch: element type and an FNV-1a hash of the length sequence.
+std::string batch_key(const size_t* lengths, size_t count, int dtype) {
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](uint64_t v) {
+        for (int i = 0; i < 8; ++i) {
+            h ^= (v >> (8 * i)) & 0xff;
+            h *= 1099511628211ull;
+        }
+    };
+    mix((uint64_t)count);
+    for (size_t i = 0; i < count; ++i) mix((uint64_t)lengths[i]);
+    char buf[64];
+    std::snprintf(buf, sizeof(buf), "batch%s:%zu:%016llx", dtype == FYG_C32 ? "32" : "64", count,
+                  (unsigned long long)h);
+    return buf;
+}
+
+// Sets the group-plan options for this thread while alive.
+struct BatchOptions {
+    BatchOptions(int radix_cap, int single_kb) { set_batch_tile_options(radix_cap, (size_t)single_kb << 10); }
+    ~BatchOptions() { set_batch_tile_options(0, 0); }
+};
+
+}  // namespace
+
 extern "C" {
 
 int fyg_batch_create(const size_t* lengths, size_t count, int dtype, int flags, fyg_batch** out) {
@@ -282,6 +312,10 @@ int fyg_batch_create(const size_t* lengths, size_t count, int dtype, int flags, 
     if (!out || (!lengths && count)) return set_error(FYG_ERR_NULL_PTR, "null argument");
     *out = nullptr;
     if (dtype != FYG_C32 && dtype != FYG_C64) return set_error(FYG_ERR_INVALID_ARG, "bad dtype");
+    TuneChoice tc;
+    if ((flags & FYG_FLAG_AUTOTUNED) && !tune_lookup_key(batch_key(lengths, count, dtype), &tc)) tc = TuneChoice();
+    flags &= ~FYG_FLAG_AUTOTUNED;
+    BatchOptions opts((int)tc.max_pass_radix, tc.cols);
     auto b = std::make_unique<fyg_batch>();
     b->dtype = dtype;
     b->flags = flags;
@@ -299,9 +333,6 @@ int fyg_batch_create(const size_t* lengths, size_t count, int dtype, int flags, 
                                  flags | FYG_FLAG_NO_L2_CHUNK | FYG_FLAG_SMALL_TILES, &p);
         if (rc) return rc;
         b->group_plans[kv.first] = p;
-        rc = fyg_plan_create(kv.first, dtype, 1, flags, &p);
-        if (rc) return rc;
-        b->single_plans[kv.first] = p;
     }
     if (dtype == FYG_C32 && count > 0) {
         int rc = build_persistent(b.get());
@@ -322,6 +353,14 @@ int fyg_batch_execute_plain(fyg_batch* b, const void* in, void* out, int directi
     clear_error();
     if (!b || !in || !out) return set_error(FYG_ERR_NULL_PTR, "null argument");
     const size_t eb = b->dtype == FYG_C32 ? 8 : 16;
+    // one plan per distinct length with batch 1, created on first use
+    for (size_t len : b->lengths) {
+        if (b->single_plans.count(len)) continue;
+        fyg_plan* p = nullptr;
+        const int rc = fyg_plan_create(len, b->dtype, 1, b->flags, &p);
+        if (rc) return rc;
+        b->single_plans[len] = p;
+    }
     for (size_t i = 0; i < b->lengths.size(); ++i) {
         const char* x = (const char*)in + b->offsets[i] * eb;
         char* y = (char*)out + b->offsets[i] * eb;
@@ -407,3 +446,62 @@ int fyg_batch_inject_stall(fyg_batch* b, int enable, int timeout_ms) {
 }
 
 }  // extern "C"
+
+// Times the persistent launch of this length sequence under each group-plan option set (stage
+// radix cap 16 or 32, single-pass tile cap 48 / 100 / 160 KB of shared memory) on random data
+// and caches the fastest; fyg_batch_create(..., FYG_FLAG_AUTOTUNED) uses it.
+extern "C" int fyg_batch_autotune(const size_t* lengths, size_t count, int dtype, const char* cache_path,
+                                  double* best_ms) {
+    clear_error();
+    if (!lengths || count == 0) return set_error(FYG_ERR_NULL_PTR, "no lengths");
+    if (dtype != FYG_C32) return set_error(FYG_ERR_UNSUPPORTED, "batch autotuning needs FYG_C32 (persistent kernel)");
+    size_t total = 0;
+    for (size_t i = 0; i < count; ++i) total += lengths[i];
+    DevBuf in, out;
+    int rc = in.alloc(total * 8);
+    if (!rc) rc = out.alloc(total * 8);
+    if (!rc) rc = fyg_fill_random_device(11, 1, dtype, total, in.ptr, nullptr);
+    if (rc) return rc;
+    const bool verbose = std::getenv("FYG_AUTOTUNE_VERBOSE") != nullptr;
+    const int cand[][2] = {{16, 100}, {32, 100}, {16, 48}, {32, 160}};
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    TuneChoice best;
+    bool have = false;
+    for (const auto& c : cand) {
+        fyg_batch* b = nullptr;
+        {
+            BatchOptions opts(c[0], c[1]);
+            if (fyg_batch_create(lengths, count, dtype, 0, &b) != FYG_OK) continue;
+        }
+        double t = 1e30;
+        bool ok = b->persistent && fyg_batch_execute(b, in.ptr, out.ptr, nullptr, FYG_FORWARD, nullptr) == FYG_OK;
+        for (int rep = 0; rep < 3 && ok; ++rep) {
+            cudaEventRecord(e0, nullptr);
+            ok = fyg_batch_execute(b, in.ptr, out.ptr, nullptr, FYG_FORWARD, nullptr) == FYG_OK;
+            cudaEventRecord(e1, nullptr);
+            ok = ok && cudaEventSynchronize(e1) == cudaSuccess && fyg_batch_status(b, nullptr) == FYG_OK;
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            t = std::min(t, (double)ms);
+        }
+        fyg_batch_destroy(b);
+        if (verbose)
+            std::fprintf(stderr, "fyg_batch_autotune radix_cap=%d single_tile_kb=%d: %s %.4f ms\n", c[0], c[1],
+                         ok ? "ok" : "failed", ok ? t : 0.0);
+        if (ok && (!have || t < best.ms)) {
+            best = TuneChoice();
+            best.max_pass_radix = (uint64_t)c[0];
+            best.cols = c[1];
+            best.ms = t;
+            have = true;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    clear_error();
+    if (!have) return set_error(FYG_ERR_UNSUPPORTED, "batch autotune: no candidate ran");
+    if (best_ms) *best_ms = best.ms;
+    return tune_store_key(batch_key(lengths, count, dtype), best, cache_path);
+}

@@ -33,6 +33,26 @@ template <typename T2, typename T> __device__ __forceinline__ T2 cscale(T2 a, T 
 // -i * a
 template <typename T2> __device__ __forceinline__ T2 mul_mi(T2 a) { return mk<T2>(a.y, -a.x); }
 
+// FP32 complex add / subtract as one packed f32x2 instruction (sm_100+): both lanes are IEEE
+// round-to-nearest operations.  Unlike the scalar form they are never contracted into an FMA
+// with a neighbouring multiply (measured: 3-5% faster passes, rel-L2 1.69e-7 -> 1.72e-7 at 2^20).
+template <> __device__ __forceinline__ float2 cadd<float2>(float2 a, float2 b) {
+    float2 d;
+    asm("{\n .reg .b64 ra, rb, rd;\n mov.b64 ra, {%2, %3};\n mov.b64 rb, {%4, %5};\n add.rn.f32x2 rd, ra, rb;\n"
+        " mov.b64 {%0, %1}, rd;\n}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+template <> __device__ __forceinline__ float2 csub<float2>(float2 a, float2 b) {
+    float2 d;
+    asm("{\n .reg .b64 ra, rb, rd;\n mov.b64 ra, {%2, %3};\n mov.b64 rb, {%4, %5};\n sub.rn.f32x2 rd, ra, rb;\n"
+        " mov.b64 {%0, %1}, rd;\n}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+
 // Conversions between storage (TIO) and compute (T) complex types.
 __device__ __forceinline__ float2 to_c(float2 v, float) { return v; }
 __device__ __forceinline__ double2 to_c(float2 v, double) { return make_double2(v.x, v.y); }

@@ -43,6 +43,11 @@ struct TuneChoice {
     double ms = 0;
 };
 bool tune_lookup(size_t n, int dtype, TuneChoice* out);
+// Autotune cache entries by key (the batch autotuner stores its choice under "batch..." keys).
+bool tune_lookup_key(const std::string& key, TuneChoice* out);
+int tune_store_key(const std::string& key, const TuneChoice& choice, const char* cache_path);
+// Options of uneven-batch group plans for plans created next on this thread (0 = defaults).
+void set_batch_tile_options(int radix_cap, size_t single_cap_bytes);
 int plan_create_opts(size_t n, int dtype, size_t batch, int flags, uint64_t max_pass_radix, uint64_t conv_length,
                      int cols, int order, fyg_plan** out);
 void host_two_level(uint64_t L, int cb, std::vector<unsigned char>& hi, std::vector<unsigned char>& lo, int* shift);

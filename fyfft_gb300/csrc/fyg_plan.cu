@@ -190,6 +190,10 @@ static const int kRadices[] = {
 // Plans of uneven batches cap the stage radix at 16 so the persistent kernel compiles only the
 // smaller codelets (lower register pressure); set for the duration of such a plan's creation.
 static thread_local int t_radix_cap = 0;
+// Uneven-batch group plans (FYG_FLAG_SMALL_TILES): stage-radix cap and single-pass tile cap
+// (bytes of shared memory), 0 = defaults (16, 100 KB); set around a batch's plan creation.
+static thread_local int t_batch_radix_cap = 0;
+static thread_local size_t t_batch_single_cap = 0;
 static int max_radix(int cb) {
     const int r = cb == 8 ? 32 : 16;
     return t_radix_cap ? std::min(r, t_radix_cap) : r;
@@ -586,7 +590,9 @@ static int make_plan(fyg_plan* pl) {
         return FYG_OK;
     }
     // ---- strategy ----
-    const size_t single_cap = (pl->flags & FYG_FLAG_SMALL_TILES) ? (100u << 10) : kSmemLimit;
+    const size_t single_cap = (pl->flags & FYG_FLAG_SMALL_TILES)
+                                  ? (t_batch_single_cap ? std::min(t_batch_single_cap, kSmemLimit) : (100u << 10))
+                                  : kSmemLimit;
     if (is_smooth(n, 13) && n <= 16384 && tile_fits(io_cb, (int)n, 1, true) &&
         smem_for(io_cb, (int)n, 1, true) <= single_cap) {
         ps.kind = GS_SINGLE;
@@ -1010,6 +1016,11 @@ fyg_plan::~fyg_plan() {
 }
 
 namespace fyg {
+void set_batch_tile_options(int radix_cap, size_t single_cap_bytes) {
+    t_batch_radix_cap = radix_cap;
+    t_batch_single_cap = single_cap_bytes;
+}
+
 // plan creation with explicit schedule options (0 = default); used by the autotuner
 int plan_create_opts(size_t n, int dtype, size_t batch, int flags, uint64_t max_pass_radix, uint64_t conv_length,
                      int cols, int order, fyg_plan** out) {
@@ -1059,7 +1070,7 @@ int fyg_plan_create(size_t n, int dtype, size_t batch, int flags, fyg_plan** out
     pl->dtype = dtype;
     pl->flags = flags;
     pl->device = dev;
-    t_radix_cap = (flags & FYG_FLAG_SMALL_TILES) ? 16 : 0;
+    t_radix_cap = (flags & FYG_FLAG_SMALL_TILES) ? (t_batch_radix_cap ? t_batch_radix_cap : 16) : 0;
     int rc = make_plan(pl);
     t_radix_cap = 0;
     if (rc) {

@@ -131,6 +131,14 @@ int fyg_plan_profile_read(fyg_plan* plan, double* total_ms, int64_t* launches, i
  * offsets given at execute time).  One persistent kernel runs them all from a device work
  * queue.  No counterpart in the reference (it runs one transform per call). */
 int fyg_batch_create(const size_t* lengths, size_t count, int dtype, int flags, fyg_batch** out);
+
+/* Measured schedule of an uneven batch (no counterpart in the reference): times the
+ * persistent launch of this length sequence under each group-plan option set (stage-radix cap
+ * 16 / 32, single-pass tile cap 48 / 100 / 160 KB of shared memory) on random device data and
+ * caches the fastest in the autotune cache (see fyg_autotune) under a key made of the element
+ * type and a hash of the lengths.  fyg_batch_create with FYG_FLAG_AUTOTUNED uses it.  FYG_C32
+ * only.  *best_ms (optional) receives the winner's milliseconds per forward execution. */
+int fyg_batch_autotune(const size_t* lengths, size_t count, int dtype, const char* cache_path, double* best_ms);
 int fyg_batch_destroy(fyg_batch* batch);
 
 /* offsets_dev: device array of `count` int64 element offsets (NULL: packed back to back in the

@@ -92,3 +92,25 @@ def test_stalled_dependency_times_out_and_context_recovers(batch):
     ys = split(y.cpu().numpy(), lengths)
     for n, xi, yi in zip(lengths[:32], split(x, lengths), ys):
         assert O.rel_l2(yi, O.fft(xi)) <= 2e-6, n
+
+
+def test_batch_autotune_caches_a_choice_and_the_tuned_batch_is_exact(tmp_path):
+    import json
+    lengths = uneven_lengths(count=160, seed=7)
+    path = str(tmp_path / "batch_tune.json")
+    ms = fg.autotune_batch(lengths, cache_path=path)
+    assert ms > 0
+    doc = json.load(open(path))
+    keys = [k for k in doc["entries"] if k.startswith("batch32:160:")]
+    assert len(keys) == 1
+    e = doc["entries"][keys[0]]
+    assert e["max_pass_radix"] in (16, 32) and e["cols"] in (48, 100, 160)
+    b = fg.UnevenBatch(lengths, flags=fg.FYG_FLAG_AUTOTUNED)
+    x = fg.fill_random(8, sum(lengths), np.complex64, "uniform")
+    xd = torch.from_numpy(x).cuda()
+    y = torch.empty_like(xd)
+    b.execute(xd, y)
+    assert b.status() == 0
+    torch.cuda.synchronize()
+    for n, xi, yi in zip(lengths, split(x, lengths), split(y.cpu().numpy(), lengths)):
+        assert O.rel_l2(yi, O.fft(xi)) <= 2e-6, n
