@@ -152,7 +152,8 @@ __global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1)) k_fast(const __gr
     const int c = threadIdx.x % C;
     const int g = threadIdx.x / C;
     // all C columns of a tile belong to one transform (Rr is a multiple of C)
-    const Col<float> ci = make_col<float, float>(p, (int64_t)blockIdx.x * C + c);
+    const unsigned tile = p.reverse_tiles ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+    const Col<float> ci = make_col<float, float>(p, (int64_t)tile * C + c);
     const float2* twl = reinterpret_cast<const float2*>(p.tw_local);
     const int Rr = p.Rr;
 

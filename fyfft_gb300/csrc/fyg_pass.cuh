@@ -100,6 +100,9 @@ struct alignas(16) PassParams {
     const void* tw_tiled;
     const void* tab_tiled;
     int tw_tile_period;
+    // register-resident kernels: 1 = tiles in reverse order (odd passes of a pipeline start on
+    // the tail the previous pass left in L2)
+    int reverse_tiles;
 };
 
 __device__ __forceinline__ int64_t transform_base(const int64_t* offs, const int* ids, int64_t b, int64_t dist) {

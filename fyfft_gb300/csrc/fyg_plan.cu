@@ -529,6 +529,7 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
             (L / R) % (uint64_t)fc == 0 && !(p.mid && (p.load_mode != LD_PLAIN || p.Ns <= 1)) &&
             (p.Ns <= 1 || p.Ns % fc == 0)) {
             fill_geom(p.g, R, fc, false, rad);
+            p.reverse_tiles = i & 1;   // measured 0.3-2% faster than one order for all passes
             d.kv = KV_FAST;
             d.threads = ft;
             d.smem = fsm;
