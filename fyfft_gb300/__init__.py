@@ -33,7 +33,7 @@ FYG_FLAG_SMALL_TILES, FYG_FLAG_AUTOTUNED, FYG_FLAG_GENERIC_KERNELS = 8, 16, 32
 
 # every symbol include/fygpu.h declares
 EXPORTED_SYMBOLS = (
-    "fyg_plan_create", "fyg_plan_create_ex", "fyg_autotune", "fyg_plan_destroy", "fyg_execute", "fyg_execute_adjoint", "fyg_strategy",
+    "fyg_plan_create", "fyg_plan_create_ex", "fyg_plan_create_layout", "fyg_autotune", "fyg_plan_destroy", "fyg_execute", "fyg_execute_adjoint", "fyg_strategy",
     "fyg_gpu_strategy", "fyg_plan_info", "fyg_plan_launches", "fyg_plan_describe", "fyg_plan_profile",
     "fyg_plan_profile_read", "fyg_batch_create", "fyg_batch_autotune", "fyg_batch_destroy",
     "fyg_batch_execute", "fyg_batch_execute_plain", "fyg_batch_status", "fyg_batch_inject_stall",
@@ -71,6 +71,7 @@ def lib() -> ctypes.CDLL:
         sz, vp, i, d, u64 = ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_uint64
         L.fyg_plan_create.argtypes = [sz, i, sz, i, ctypes.POINTER(vp)]
         L.fyg_plan_create_ex.argtypes = [sz, i, sz, i, sz, sz, ctypes.POINTER(vp)]
+        L.fyg_plan_create_layout.argtypes = [sz, i, sz, sz, sz, i, ctypes.POINTER(vp)]
         L.fyg_autotune.argtypes = [sz, i, sz, ctypes.c_char_p, ctypes.POINTER(d)]
         L.fyg_plan_destroy.argtypes = [vp]
         L.fyg_execute.argtypes = [vp, vp, vp, i, vp]
@@ -188,12 +189,17 @@ class FFT1D_C2C_invoker:
     FFT_execution_strategy = FFT_execution_strategy
 
     def __init__(self, length: int, dtype="complex64", batch: int = 1, flags: int = 0,
-                 max_pass_radix: int = 0, conv_length: int = 0):
+                 max_pass_radix: int = 0, conv_length: int = 0, idist: int = 0, odist: int = 0):
         self.N = int(length)
         self.batch = int(batch)
+        self.idist = int(idist) or self.N
+        self.odist = int(odist) or self.N
         self.dtype_code = FYG_C32 if str(dtype).endswith("complex64") else FYG_C64
         h = ctypes.c_void_p()
-        if max_pass_radix or conv_length:
+        if idist or odist:
+            check(lib().fyg_plan_create_layout(self.N, self.dtype_code, self.batch, int(idist), int(odist), flags,
+                                               ctypes.byref(h)))
+        elif max_pass_radix or conv_length:
             check(lib().fyg_plan_create_ex(self.N, self.dtype_code, self.batch, flags, int(max_pass_radix),
                                            int(conv_length), ctypes.byref(h)))
         else:
@@ -214,11 +220,12 @@ class FFT1D_C2C_invoker:
     def _io(self, x, y):
         px, nx, dx, _ = _buffer_ptr(x)
         py, ny, dy, _ = _buffer_ptr(y)
-        need = self.N * self.batch
+        need_x = (self.batch - 1) * self.idist + self.N
+        need_y = (self.batch - 1) * self.odist + self.N
         if dx != self.dtype_code or dy != self.dtype_code:
             raise TypeError("buffer dtype does not match the plan")
-        if nx < need or ny < need:
-            raise ValueError(f"buffers hold {nx}/{ny} complex elements, plan needs {need}")
+        if nx < need_x or ny < need_y:
+            raise ValueError(f"buffers hold {nx}/{ny} complex elements, plan needs {need_x}/{need_y}")
         return px, py
 
     def dispatch(self, invert: bool, input, output, stream=None) -> None:

@@ -118,6 +118,21 @@ __device__ __forceinline__ void fast_stages_from(float2 (&v)[S::P], float2* sm, 
     }
 }
 
+// L2 residency: the thread-order tables are read by every transform of a batch, the streamed
+// data once; table reads carry an evict-last policy so the tables stay in L2 while the batch
+// streams through it (measured: Bluestein 999983 -2.6%, 131074 -4%; evict-first data loads
+// were slower and are not used).
+__device__ __forceinline__ uint64_t l2_keep_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ float2 ld_table(const float2* ptr, uint64_t pol) {
+    float2 v;
+    asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(ptr), "l"(pol));
+    return v;
+}
+
 // Load variants, compiled as separate kernels so that each gets its own register allocation.
 enum FastLoad : int {
     FL_PLAIN = 0,     // x (conjugated for inverses): first passes
@@ -156,6 +171,7 @@ __global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1)) k_fast(const __gr
     const Col<float> ci = make_col<float, float>(p, (int64_t)tile * C + c);
     const float2* twl = reinterpret_cast<const float2*>(p.tw_local);
     const int Rr = p.Rr;
+    const uint64_t keep = l2_keep_policy();
 
     // ---- load: register i <- x[jj + n Rr], n = g + G i ----
     float2 v[P];
@@ -176,7 +192,7 @@ __global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1)) k_fast(const __gr
 #pragma unroll
             for (int i = 0; i < P; ++i) {
                 const int gidx = ci.jj + (g + G * i) * Rr;
-                const float2 u = cmul(make_float2(v[i].x, v[i].y * isign), __ldg(tab + i * S::T));
+                const float2 u = cmul(make_float2(v[i].x, v[i].y * isign), ld_table(tab + i * S::T, keep));
                 v[i] = gidx <= nlast ? u : make_float2(0.f, 0.f);
             }
         } else {
@@ -213,7 +229,7 @@ __global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1)) k_fast(const __gr
                 const float2* tw = reinterpret_cast<const float2*>(p.tw_tiled) +
                                    (size_t)((ci.jj / C) % p.tw_tile_period) * (P * S::T) + threadIdx.x;
 #pragma unroll
-                for (int i = 0; i < P; ++i) v[i] = cmul(v[i], __ldg(tw + i * S::T));
+                for (int i = 0; i < P; ++i) v[i] = cmul(v[i], ld_table(tw + i * S::T, keep));
             } else if (ci.k) {
                 fast_twiddle<P, G, S::TWB>(v, p, g, (uint32_t)ci.k * (uint32_t)p.Lr);
             }
@@ -231,7 +247,7 @@ __global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1)) k_fast(const __gr
         if (p.tab_tiled) {
             const float2* tab = reinterpret_cast<const float2*>(p.tab_tiled) + (size_t)(ci.jj / C) * (P * S::T) + threadIdx.x;
 #pragma unroll
-            for (int i = 0; i < P; ++i) v[i] = cconj(cmul(v[i], __ldg(tab + i * S::T)));
+            for (int i = 0; i < P; ++i) v[i] = cconj(cmul(v[i], ld_table(tab + i * S::T, keep)));
         } else {
 #pragma unroll
             for (int i = 0; i < P; ++i) v[i] = cconj(cmul(v[i], __ldg(spec + ci.jj + (g + G * i) * Rr)));
@@ -267,7 +283,7 @@ __global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1)) k_fast(const __gr
 #pragma unroll
             for (int i = 0; i < P; ++i) {
                 const int oidx = ci.out_j + (g + G * i) * ns;
-                const float2 w = p.tab_tiled ? __ldg(tab + i * S::T) : __ldg(chirp + min(oidx, nlast));
+                const float2 w = p.tab_tiled ? ld_table(tab + i * S::T, keep) : __ldg(chirp + min(oidx, nlast));
                 const float2 u = cmul(w, v[i]);
                 if (oidx <= nlast) dst[(g + G * i) * ns] = make_float2(u.x * scale, u.y * sy);
             }

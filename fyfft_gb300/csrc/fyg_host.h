@@ -50,6 +50,8 @@ int tune_store_key(const std::string& key, const TuneChoice& choice, const char*
 void set_batch_tile_options(int radix_cap, size_t single_cap_bytes);
 int plan_create_opts(size_t n, int dtype, size_t batch, int flags, uint64_t max_pass_radix, uint64_t conv_length,
                      int cols, int order, fyg_plan** out);
+// Layout of the user buffers of plans created next on this thread (0 = contiguous).
+void set_plan_layout(size_t idist, size_t odist);
 void host_two_level(uint64_t L, int cb, std::vector<unsigned char>& hi, std::vector<unsigned char>& lo, int* shift);
 
 // GPU-side strategy of a plan (what actually runs).
@@ -103,6 +105,7 @@ struct fyg_plan_impl;
 // The opaque plan type of the C ABI.
 struct fyg_plan {
     size_t n = 0, batch = 0;
+    size_t idist = 0, odist = 0;   // elements between the starts of consecutive user transforms
     int dtype = FYG_C32;
     int flags = 0;
     int device = 0;

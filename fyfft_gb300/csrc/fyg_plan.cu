@@ -263,6 +263,7 @@ bool tile_fits(int cb, int R, int C, bool colmajor) {
 static thread_local uint64_t t_max_pass_r = 0;
 static thread_local uint64_t t_conv_len = 0;
 static thread_local int t_order = 0;  // 1: reversed pass order
+static thread_local size_t t_idist = 0, t_odist = 0;  // user layout of the next plan (0: contiguous)
 static thread_local int t_cols = 0;   // single-pass: transforms per CTA (threads per transform = T/C)
 
 bool split_passes(uint64_t L, int cb, bool conv, std::vector<int>& out) {
@@ -488,8 +489,8 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
         d.out_role = last ? ROLE_OUT : (i % 2 == 0 ? ROLE_S0 : ROLE_S1);
         d.in_elem_bytes = d.in_role == ROLE_IN ? io_cb : cb;
         d.out_elem_bytes = d.out_role == ROLE_OUT ? io_cb : cb;
-        p.idist = d.in_role == ROLE_IN ? (int64_t)n : (int64_t)L;
-        p.odist = d.out_role == ROLE_OUT ? (int64_t)n : (int64_t)L;
+        p.idist = d.in_role == ROLE_IN ? (int64_t)pl->idist : (int64_t)L;
+        p.odist = d.out_role == ROLE_OUT ? (int64_t)pl->odist : (int64_t)L;
         // load / store fusions
         p.load_mode = LD_PLAIN;
         p.store_mode = ST_PLAIN;
@@ -810,8 +811,8 @@ static int run_pipeline(fyg_plan* pl, const std::vector<PassDesc>& pipe, const v
             PassParams p = d.p;
             auto resolve = [&](int role) -> void* {
                 switch (role) {
-                    case ROLE_IN: return (void*)((const char*)in + c0 * pl->n * io_cb);
-                    case ROLE_OUT: return (void*)((char*)out + c0 * pl->n * io_cb);
+                    case ROLE_IN: return (void*)((const char*)in + c0 * pl->idist * io_cb);
+                    case ROLE_OUT: return (void*)((char*)out + c0 * pl->odist * io_cb);
                     case ROLE_S0: return pl->scratch0.ptr;
                     default: return pl->scratch1.ptr;
                 }
@@ -863,18 +864,38 @@ static bool is_device_ptr(const void* ptr) {
 // stream), its kernels (the caller's stream) and its device->host copy (copy-out stream) are
 // ordered by events, so copies in both directions overlap the kernels of neighbouring chunks.
 // Returns when the output is in host memory.
+// Bytes of a user buffer: the last transform's start plus one transform.
+static size_t span_bytes(const fyg_plan* pl, size_t dist) {
+    const size_t cb = pl->dtype == FYG_C32 ? 8 : 16;
+    return ((pl->batch - 1) * dist + pl->n) * cb;
+}
+
+// Copies transforms [b0, b0 + nb) of a user layout (rows of n elements, `dist` apart), leaving
+// the gaps between transforms untouched: one 1D copy when the rows are back to back.
+static cudaError_t copy_rows(void* dst, const void* src, const fyg_plan* pl, size_t dist, size_t b0, size_t nb,
+                             cudaMemcpyKind kind, cudaStream_t st) {
+    const size_t cb = pl->dtype == FYG_C32 ? 8 : 16;
+    const size_t off = b0 * dist * cb, w = pl->n * cb, pitch = dist * cb;
+    char* d = static_cast<char*>(dst) + off;
+    const char* s = static_cast<const char*>(src) + off;
+    if (pitch == w) return cudaMemcpyAsync(d, s, nb * w, kind, st);
+    return cudaMemcpy2DAsync(d, pitch, s, pitch, w, nb, kind, st);
+}
+
+static int ensure_staging(fyg_plan* pl) {
+    const size_t need = std::max(span_bytes(pl, pl->idist), span_bytes(pl, pl->odist));
+    if (pl->stage_in_bytes >= need) return FYG_OK;
+    int rc = pl->stage_in.alloc(need);
+    if (!rc) rc = pl->stage_out.alloc(need);
+    if (rc) return rc;
+    pl->stage_in_bytes = need;
+    return FYG_OK;
+}
+
 static int execute_host_overlapped(fyg_plan* pl, const void* in, void* out, bool inverse, double scale_mul,
                                    cudaStream_t st) {
-    const int io_cb = pl->dtype == FYG_C32 ? 8 : 16;
-    const size_t per = pl->n * (size_t)io_cb;
-    const size_t bytes = per * pl->batch;
-    int rc = FYG_OK;
-    if (pl->stage_in_bytes < bytes) {
-        rc = pl->stage_in.alloc(bytes);
-        if (!rc) rc = pl->stage_out.alloc(bytes);
-        if (rc) return rc;
-        pl->stage_in_bytes = bytes;
-    }
+    int rc = ensure_staging(pl);
+    if (rc) return rc;
     // about 8 chunks, whole transforms, at least one L2 chunk of the plan each
     size_t cb = std::max<size_t>((pl->batch + 7) / 8, 1);
     if (pl->chunk < pl->batch) cb = std::max(cb, pl->chunk) / pl->chunk * pl->chunk;
@@ -902,15 +923,14 @@ static int execute_host_overlapped(fyg_plan* pl, const void* in, void* out, bool
     for (size_t i = 0; i < nch && !rc; ++i) {
         const size_t b0 = i * cb, nb = std::min(cb, pl->batch - b0);
         cudaEvent_t ev_in = pl->stage_ev[2 * i], ev_done = pl->stage_ev[2 * i + 1];
-        rc = chk(cudaMemcpyAsync(sin + b0 * per, hin + b0 * per, nb * per, cudaMemcpyHostToDevice, pl->s_h2d),
-                 "host->device staging");
+        rc = chk(copy_rows(sin, hin, pl, pl->idist, b0, nb, cudaMemcpyHostToDevice, pl->s_h2d), "host->device staging");
         if (!rc) rc = chk(cudaEventRecord(ev_in, pl->s_h2d), "event");
         if (!rc) rc = chk(cudaStreamWaitEvent(st, ev_in, 0), "wait");
         if (!rc) rc = run_pipeline(pl, inverse ? pl->inv : pl->fwd, sin, sout, scale_mul, st, b0, b0 + nb);
         if (!rc) rc = chk(cudaEventRecord(ev_done, st), "event");
         if (!rc) rc = chk(cudaStreamWaitEvent(pl->s_d2h, ev_done, 0), "wait");
         if (!rc)
-            rc = chk(cudaMemcpyAsync(hout + b0 * per, sout + b0 * per, nb * per, cudaMemcpyDeviceToHost, pl->s_d2h),
+            rc = chk(copy_rows(hout, sout, pl, pl->odist, b0, nb, cudaMemcpyDeviceToHost, pl->s_d2h),
                      "device->host staging");
     }
     // always drain both copy streams before returning (the host buffers are the caller's)
@@ -930,6 +950,8 @@ static int execute_dir(fyg_plan* pl, const void* in, void* out, bool inverse, do
     int cur = 0;
     cudaGetDevice(&cur);
     if (cur != pl->device) cudaSetDevice(pl->device);
+    if (in == out && pl->idist != pl->odist)
+        return set_error(FYG_ERR_INVALID_ARG, "in-place execution needs equal input and output distances");
     const size_t bytes = pl->n * pl->batch * io_cb;
     const bool din = is_device_ptr(in), dout = is_device_ptr(out);
     if (!din && !dout && pl->strategy != GS_COPY && pl->batch >= 2 && bytes >= (8u << 20)) {
@@ -941,14 +963,10 @@ static int execute_dir(fyg_plan* pl, const void* in, void* out, bool inverse, do
     void* dout_p = out;
     int rc = FYG_OK;
     if (!din || !dout) {
-        if (pl->stage_in_bytes < bytes) {
-            rc = pl->stage_in.alloc(bytes);
-            if (!rc) rc = pl->stage_out.alloc(bytes);
-            if (rc) return rc;
-            pl->stage_in_bytes = bytes;
-        }
+        rc = ensure_staging(pl);
+        if (rc) return rc;
         if (!din) {
-            cudaError_t e = cudaMemcpyAsync(pl->stage_in.ptr, in, bytes, cudaMemcpyHostToDevice, st);
+            cudaError_t e = copy_rows(pl->stage_in.ptr, in, pl, pl->idist, 0, pl->batch, cudaMemcpyHostToDevice, st);
             if (e != cudaSuccess) return cuda_error(e, "host->device staging");
             din_p = pl->stage_in.ptr;
         }
@@ -962,7 +980,7 @@ static int execute_dir(fyg_plan* pl, const void* in, void* out, bool inverse, do
         if (rc) return rc;
     }
     if (!dout) {
-        cudaError_t e = cudaMemcpyAsync(out, dout_p, bytes, cudaMemcpyDeviceToHost, st);
+        cudaError_t e = copy_rows(out, dout_p, pl, pl->odist, 0, pl->batch, cudaMemcpyDeviceToHost, st);
         if (e != cudaSuccess) return cuda_error(e, "device->host staging");
     }
     if (!din || !dout) {
@@ -977,7 +995,9 @@ static int gpu_fft_f64(size_t n, const std::vector<double2>& h, std::vector<doub
     fyg_plan* sub = nullptr;
     const uint64_t keep_r = t_max_pass_r, keep_m = t_conv_len;
     const int keep_order = t_order;
+    const size_t keep_idist = t_idist, keep_odist = t_odist;
     t_order = 0;
+    t_idist = t_odist = 0;
     const int keep_cap = t_radix_cap, keep_cols = t_cols;
     t_max_pass_r = t_conv_len = 0;
     t_radix_cap = t_cols = 0;
@@ -985,6 +1005,8 @@ static int gpu_fft_f64(size_t n, const std::vector<double2>& h, std::vector<doub
     t_max_pass_r = keep_r;
     t_conv_len = keep_m;
     t_order = keep_order;
+    t_idist = keep_idist;
+    t_odist = keep_odist;
     t_radix_cap = keep_cap;
     t_cols = keep_cols;
     if (rc) return rc;
@@ -1017,6 +1039,11 @@ fyg_plan::~fyg_plan() {
 }
 
 namespace fyg {
+void set_plan_layout(size_t idist, size_t odist) {
+    t_idist = idist;
+    t_odist = odist;
+}
+
 void set_batch_tile_options(int radix_cap, size_t single_cap_bytes) {
     t_batch_radix_cap = radix_cap;
     t_batch_single_cap = single_cap_bytes;
@@ -1039,6 +1066,18 @@ int plan_create_opts(size_t n, int dtype, size_t batch, int flags, uint64_t max_
 }  // namespace fyg
 
 extern "C" {
+
+int fyg_plan_create_layout(size_t n, int dtype, size_t batch, size_t idist, size_t odist, int flags, fyg_plan** out) {
+    clear_error();
+    if (idist && idist < n) return set_error(FYG_ERR_INVALID_ARG, "idist must be 0 or >= n");
+    if (odist && odist < n) return set_error(FYG_ERR_INVALID_ARG, "odist must be 0 or >= n");
+    if (n == 1 && ((idist && idist != 1) || (odist && odist != 1)))
+        return set_error(FYG_ERR_UNSUPPORTED, "strided layouts need n >= 2");
+    set_plan_layout(idist, odist);
+    const int rc = fyg_plan_create(n, dtype, batch, flags, out);
+    set_plan_layout(0, 0);
+    return rc;
+}
 
 int fyg_plan_create_ex(size_t n, int dtype, size_t batch, int flags, size_t max_pass_radix, size_t conv_length,
                        fyg_plan** out) {
@@ -1068,6 +1107,8 @@ int fyg_plan_create(size_t n, int dtype, size_t batch, int flags, fyg_plan** out
     auto* pl = new fyg_plan();
     pl->n = n;
     pl->batch = batch;
+    pl->idist = t_idist ? t_idist : n;
+    pl->odist = t_odist ? t_odist : n;
     pl->dtype = dtype;
     pl->flags = flags;
     pl->device = dev;

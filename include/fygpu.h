@@ -109,6 +109,12 @@ int fyg_gpu_strategy(size_t n);
  * passes per direction, and the GPU strategy. */
 int fyg_plan_info(const fyg_plan* plan, size_t* conv_length, int* passes, int* strategy);
 
+/* Plan whose user buffers hold the batch's transforms `idist` (input) and `odist` (output)
+ * elements apart (0 = n, contiguous; otherwise >= n).  The elements between transforms are
+ * neither read nor written, for device and host buffers alike.  In-place execution needs
+ * idist == odist.  No counterpart in the reference (one contiguous transform per call). */
+int fyg_plan_create_layout(size_t n, int dtype, size_t batch, size_t idist, size_t odist, int flags, fyg_plan** out);
+
 /* Kernel launches one fyg_execute of this plan issues (passes x L2 chunks). */
 int fyg_plan_launches(const fyg_plan* plan, int* launches);
 

@@ -1,0 +1,80 @@
+"""Strided batch layout (fyg_plan_create_layout): transforms idist / odist elements apart in the
+user buffers; every transform matches the FP64 oracle and the gaps between transforms keep
+their contents, for device buffers and for host buffers (plain and overlapped staging)."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import fyfft_gb300 as fg  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+SENTINEL = np.complex64(123.0 - 45.0j)
+
+
+def strided(x, n, batch, dist):
+    buf = np.full((batch - 1) * dist + n, SENTINEL, dtype=np.complex64)
+    for b in range(batch):
+        buf[b * dist:b * dist + n] = x[b]
+    return buf
+
+
+def rows(buf, n, batch, dist):
+    return np.stack([buf[b * dist:b * dist + n] for b in range(batch)])
+
+
+def gaps_intact(buf, n, batch, dist):
+    mask = np.ones(buf.size, dtype=bool)
+    for b in range(batch):
+        mask[b * dist:b * dist + n] = False
+    return np.all(buf[mask] == SENTINEL)
+
+
+# single-pass tile (4096), Rader single pass (1009), register-resident passes (2^20, Rader
+# 65537, Bluestein 999983), generic multi-pass (10000 = 100 x 100)
+@pytest.mark.parametrize("n", [4096, 1009, 10000, 1 << 20, 65537, 999983])
+@pytest.mark.parametrize("where", ["device", "host"])
+@pytest.mark.parametrize("inverse", [False, True])
+def test_strided_layout(n, where, inverse):
+    batch, idist, odist = 3, n + 37, n + 101
+    x = fg.fill_random(17, n * batch, np.complex64, "normal").reshape(batch, n)
+    xin = strided(x, n, batch, idist)
+    yout = np.full((batch - 1) * odist + n, SENTINEL, dtype=np.complex64)
+    plan = fg.FFT1D_C2C_invoker(n, "complex64", batch, idist=idist, odist=odist)
+    if where == "device":
+        xd = torch.from_numpy(xin).cuda()
+        yd = torch.from_numpy(yout).cuda()
+        plan.dispatch(inverse, xd, yd)
+        torch.cuda.synchronize()
+        y = yd.cpu().numpy()
+        assert np.array_equal(xd.cpu().numpy(), xin)      # the input is not modified
+    else:
+        plan.dispatch(inverse, xin, yout)
+        y = yout
+    assert gaps_intact(y, n, batch, odist)
+    for b, yb in enumerate(rows(y, n, batch, odist)):
+        assert O.rel_l2(yb, O.fft(x[b], inverse=inverse)) <= 2e-6, (n, b)
+
+
+def test_layout_in_place_needs_equal_distances():
+    n, batch = 4096, 2
+    plan = fg.FFT1D_C2C_invoker(n, "complex64", batch, idist=n + 8, odist=n + 16)
+    buf = torch.zeros((batch - 1) * (n + 16) + n, dtype=torch.complex64, device="cuda")
+    with pytest.raises(fg.FygError):
+        plan.dispatch(False, buf, buf)
+    same = fg.FFT1D_C2C_invoker(n, "complex64", batch, idist=n + 8, odist=n + 8)
+    x = fg.fill_random(3, n * batch, np.complex64, "normal").reshape(batch, n)
+    b2 = torch.from_numpy(strided(x, n, batch, n + 8)).cuda()
+    same.dispatch(False, b2, b2)
+    torch.cuda.synchronize()
+    y = b2.cpu().numpy()
+    assert gaps_intact(y, n, batch, n + 8)
+    for b, yb in enumerate(rows(y, n, batch, n + 8)):
+        assert O.rel_l2(yb, O.fft(x[b])) <= 2e-6
+
+
+def test_layout_rejects_short_distances():
+    with pytest.raises(fg.FygError):
+        fg.FFT1D_C2C_invoker(4096, "complex64", 2, idist=4000)
