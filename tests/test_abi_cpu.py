@@ -4,6 +4,8 @@ behaves.  No GPU compute calls."""
 import ctypes
 import os
 import re
+import shutil
+import subprocess
 
 import numpy as np
 import pytest
@@ -12,6 +14,8 @@ import fyfft_gb300 as fg
 from oracle import oracle as O
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HERE = os.path.join(ROOT, "tests")
+INCLUDE = os.path.join(ROOT, "include")
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -74,3 +78,23 @@ def test_plan_create_rejects_bad_arguments_without_gpu():
 def test_oracle_and_library_agree_on_reference_strategy_samples():
     for n in (4096, 2520, 59049, 117649, 1009, 39062, 39063, 65537):
         assert fg.lib().fyg_strategy(n) == O.strategy(n)
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="needs gcc")
+def test_c_abi_header_is_plain_c99(tmp_path):
+    # the boundary header uses only C types: it compiles as strict C99
+    src = tmp_path / "h.c"
+    src.write_text('#include "fygpu.h"\nint main(void) { return FYG_OK; }\n')
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", INCLUDE,
+                        "-fsyntax-only", str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_dropin_header_example_links(tmp_path):
+    # the reference-API example program compiles against foye_FFT_gpu.hpp and links the library
+    exe = tmp_path / "dropin"
+    r = subprocess.run(["g++", "-std=c++17", "-I", INCLUDE, os.path.join(HERE, "cpp", "dropin_example.cpp"),
+                        "-L", os.path.dirname(fg.LIB_PATH), "-lfygpu", f"-Wl,-rpath,{os.path.dirname(fg.LIB_PATH)}",
+                        "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
