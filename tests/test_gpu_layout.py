@@ -32,9 +32,9 @@ def gaps_intact(buf, n, batch, dist):
     return np.all(buf[mask] == SENTINEL)
 
 
-# single-pass tile (4096), Rader single pass (1009), register-resident passes (2^20, Rader
-# 65537, Bluestein 999983), generic multi-pass (10000 = 100 x 100)
-@pytest.mark.parametrize("n", [4096, 1009, 10000, 1 << 20, 65537, 999983])
+# single-pass tile (4096), Rader single pass (1009), generic multi-pass (10000 = 100 x 100),
+# register-resident passes (2^16, Rader 65537, Bluestein 40009 on 2^17)
+@pytest.mark.parametrize("n", [4096, 1009, 10000, 1 << 16, 65537, 40009])
 @pytest.mark.parametrize("where", ["device", "host"])
 @pytest.mark.parametrize("inverse", [False, True])
 def test_strided_layout(n, where, inverse):
@@ -56,6 +56,20 @@ def test_strided_layout(n, where, inverse):
     assert gaps_intact(y, n, batch, odist)
     for b, yb in enumerate(rows(y, n, batch, odist)):
         assert O.rel_l2(yb, O.fft(x[b], inverse=inverse)) <= 2e-6, (n, b)
+
+
+def test_strided_layout_overlapped_host_staging():
+    # 3 x 2^20 complex<float> = 25 MB: host buffers go through the chunked copy/compute pipeline
+    n, batch, idist, odist = 1 << 20, 3, (1 << 20) + 64, (1 << 20) + 96
+    x = fg.fill_random(19, n * batch, np.complex64, "normal").reshape(batch, n)
+    xin = strided(x, n, batch, idist)
+    yout = np.full((batch - 1) * odist + n, SENTINEL, dtype=np.complex64)
+    plan = fg.FFT1D_C2C_invoker(n, "complex64", batch, idist=idist, odist=odist)
+    plan.dispatch(False, xin, yout)
+    assert gaps_intact(yout, n, batch, odist)
+    ys = rows(yout, n, batch, odist)
+    for b in (0, batch - 1):
+        assert O.rel_l2(ys[b], O.fft(x[b])) <= 2e-6
 
 
 def test_layout_in_place_needs_equal_distances():
