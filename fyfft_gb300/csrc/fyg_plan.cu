@@ -947,18 +947,23 @@ static int execute_dir(fyg_plan* pl, const void* in, void* out, bool inverse, do
     const int io_cb = pl->dtype == FYG_C32 ? 8 : 16;
     if (((uintptr_t)in % io_cb) || ((uintptr_t)out % io_cb))
         return set_error(FYG_ERR_MISALIGNED, "buffers must be aligned to the complex element size");
-    int cur = 0;
-    cudaGetDevice(&cur);
-    if (cur != pl->device) cudaSetDevice(pl->device);
     if (in == out && pl->idist != pl->odist)
         return set_error(FYG_ERR_INVALID_ARG, "in-place execution needs equal input and output distances");
+    // the plan's device for the duration of the call; the caller's device again on every return
+    struct DeviceScope {
+        int prev = 0, dev;
+        explicit DeviceScope(int d) : dev(d) {
+            cudaGetDevice(&prev);
+            if (prev != dev) cudaSetDevice(dev);
+        }
+        ~DeviceScope() {
+            if (prev != dev) cudaSetDevice(prev);
+        }
+    } scope(pl->device);
     const size_t bytes = pl->n * pl->batch * io_cb;
     const bool din = is_device_ptr(in), dout = is_device_ptr(out);
-    if (!din && !dout && pl->strategy != GS_COPY && pl->batch >= 2 && bytes >= (8u << 20)) {
-        const int rc = execute_host_overlapped(pl, in, out, inverse, scale_mul, st);
-        if (cur != pl->device) cudaSetDevice(cur);
-        return rc;
-    }
+    if (!din && !dout && pl->strategy != GS_COPY && pl->batch >= 2 && bytes >= (8u << 20))
+        return execute_host_overlapped(pl, in, out, inverse, scale_mul, st);
     const void* din_p = in;
     void* dout_p = out;
     int rc = FYG_OK;
@@ -987,7 +992,6 @@ static int execute_dir(fyg_plan* pl, const void* in, void* out, bool inverse, do
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return cuda_error(e, "stream synchronize");
     }
-    if (cur != pl->device) cudaSetDevice(cur);
     return FYG_OK;
 }
 
