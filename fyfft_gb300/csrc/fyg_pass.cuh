@@ -15,8 +15,10 @@
 // (src/foye_FFT_mix_radix.hpp:16-83, :536-574) and its radix engines' bit/digit-reversal LUTs:
 // Stockham indexing sorts itself.
 //
-// Inside the CTA the length-R DFT is again a Stockham sweep over radix-r stages run in place in
-// shared memory, between a coalesced load phase and a coalesced store phase (fyg_kernels.cuh).
+// Inside the CTA the length-R DFT is again a Stockham sweep over radix-r stages: ping-ponging
+// in shared memory between a coalesced load phase and a coalesced store phase (the tile kernel,
+// fyg_kernels.cuh), or on points held in registers with one shared exchange per stage (the
+// register-resident kernels, fyg_fast.cuh).
 //
 // Fusions (all selected by uniform runtime fields):
 //   load  LD_PLAIN   x (optionally conjugated)

@@ -2,21 +2,25 @@
 //
 // Plan construction replaces fy::fft::FFT1D_C2C_invoker's constructor (foye_FFT.hpp:101-126):
 // the strategy is chosen once, the stage schedule is derived from N's factorization, and all
-// tables (twiddles, chirp, Rader permutations, convolution spectra) are computed once on the
-// host in long double (spectra: FP64 GPU FFT of the long-double kernel) and uploaded.
+// tables (twiddles, chirp, Rader permutations, convolution spectra) are computed once, on the
+// host in long double (spectra: FP64 GPU FFT of the long-double kernel) and uploaded, or on the
+// device from FP64 sincospi (the thread-order tables of the register-resident kernels).
+// Each pass runs the register-resident kernel of its tile length when there is one
+// (fyg_fast.cuh: FP32, 256-4096 / 243 / 343 points), else the shared-memory tile kernel.
 //
 // GPU strategies:
 //   single    N <= one CTA's capacity and 13-smooth: one tile pass, several transforms per CTA
 //             (replaces the smooth registry's radix engines and micro-kernels,
 //             src/foye_FFT_radix_wrap.hpp:6-124, src/foye_FFT_radix{2,3,4,5,7}.hpp,
 //             src/foye_FFT_microKernel.hpp, and the batch kernel src/foye_FFT_batch_kernel.hpp)
-//   multi     13-smooth N above that: 2-3 Stockham passes of radix <= ~1800 with the inter-pass
+//   multi     13-smooth N above that: 2-3 Stockham passes of radix <= 4096 with the inter-pass
 //             twiddle fused into the next pass's load (replaces the mixed-radix planner and
 //             executor, src/foye_FFT_mix_radix.hpp:253-574)
 //   rader     prime N with 13-smooth N-1: cyclic convolution of length N-1; other primes up to
 //             the reference's Rader limit (39064): zero-padded linear convolution of 7-smooth
 //             length M >= 2N-3 (src/foye_FFT_rader.hpp:142-401)
-//   bluestein everything else: chirp-z with 7-smooth M >= 2N-1 (src/foye_FFT_bluestein.hpp:79-355)
+//   bluestein everything else: chirp-z with M >= 2N-1, the next power of two for FP32 when
+//             M >= 65536 (register-resident passes), else 7-smooth (src/foye_FFT_bluestein.hpp:79-355)
 // The reference's O(N^2) DFT fallback (src/foye_FFT_dft.hpp) is never used.
 #include <algorithm>
 #include <cmath>
