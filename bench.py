@@ -9,12 +9,20 @@ transform; GB/s with 2 N sizeof(complex) bytes per transform; fraction of the me
 roofline.  Inputs (1.24 GB per step) are larger than L2, so no flush is needed.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload sweep|c1|c5|uneven]
+                  [--workload sweep|c1|c5]
+
+The default run also reports, as extra keys of the same JSON line: the same figure over the
+lengths the reference can run (ref_runnable_subset), the other configurations timed on their
+own (configs: C1 complex<double> 4096 x 256, C4 forward + adjoint, C5 2^27 x 1 and 2^24 x 8, each
+with its dominant pass's roofline), the mixed-length batch in one persistent launch against one
+launch sequence per plan (batched_vs_plain), and the CPU baseline with the GPU's rel-L2 against
+the reference and the FP64 oracle.
 
 N > 1 runs one independent replica per GPU (the path does not shard): value is the total
-over ranks divided by the max time over ranks.  --impl reference times the CPU restatement of
-the reference's algorithm (oracle/, FP64) on the host cores on a bounded sample of the same
-workload (the reference's own AVX2 code is x86-only).
+over ranks divided by the max time over ranks.  --impl reference times the reference's own
+C++ FFT (oracle/_ref/libfyref.so: the unmodified reference, built natively with AVX2 on x86-64
+and against oracle/ref/portable_intrin.h on the aarch64 GPU hosts) on all host cores, one plan
+per thread, over the whole batch of every workload length it can run.
 """
 from __future__ import annotations
 
@@ -222,26 +230,10 @@ def run_ours(args, rank: int, world: int):
     value = step_flops * world / (ms_step * 1e-3) / 1e9
 
     # dominant kernel: the pass with the largest accumulated time
-    best = None
-    for (n, b, *_ ), p in zip(items, plans):
-        for i, (tms, nl, bpl) in enumerate(p.profile_read()):
-            if nl and (best is None or tms > best[0]):
-                best = (tms, nl, bpl, n, i, len(p.profile_read()), p.describe()[i])
-        p.profile(False)
-    roof = None
-    if best:
-        tms, nl, bpl, n, i, npass, pdesc = best
-        kind = "k_fast" if "kernel=fast" in pdesc else "k_pass"
-        shape = " ".join(w for w in pdesc.split() if w.startswith(("R=", "C=")))
-        avg_ms = tms / nl
-        achieved = bpl / (avg_ms * 1e-3) / 1e9
-        share = tms / (ms_total if ms_total > 0 else 1)
-        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
-                "frac": round(achieved / hbm_peak, 3), "traffic": read_traffic(n, i),
-                "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else peak_src,
-                "kernel": f"{kind} {shape} (N={n} pass {i + 1}/{npass}{', mid' if ' mid' in pdesc else ''})",
-                "bytes_per_launch": int(bpl),
-                "avg_launch_ms": round(avg_ms, 4), "share_of_step": round(share, 3)}
+    roof = dominant_pass([(n, p) for (n, *_ ), p in zip(items, plans)], ms_total, hbm_peak)
+    if roof:
+        roof["peak_source"] = f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else peak_src
+        roof["share_of_step"] = roof.pop("share")
 
     # end to end through the public API with pinned host buffers (H2D + compute + D2H per step)
     # each step timed on its own; the value uses the median step (host-side copy bandwidth on a
@@ -321,11 +313,126 @@ def run_ours(args, rank: int, world: int):
         "clocks": clk,
         "per_size": per_size,
     }
+    # the same figure over the lengths the reference can run (the reference arm's value is
+    # taken over those; 65537, 999983 and 131074 fall to its O(N^2) DFT)
+    sub = [(n, b) for (n, b, *_ ) in items if n in REF_RUNNABLE]
+    if sub:
+        sub_ms = sum(per_size[str(n)]["ms"] for n, _ in sub)
+        out["ref_runnable_subset"] = {
+            "sizes": [n for n, _ in sub],
+            "value": round(sum(flops(n) * b for n, b in sub) / (sub_ms * 1e-3) / 1e9, 1), "unit": "GFLOP/s",
+            "ms_per_step": round(sub_ms, 4), "from": "per_size device times (events, 5 repetitions each)"}
+    uneven = None
     if not args.no_uneven:
-        out["batched_vs_plain"] = uneven_batch(dev, stream, no_autotune=args.no_autotune)
+        out["batched_vs_plain"], uneven = uneven_batch(dev, stream, no_autotune=args.no_autotune)
+    if not args.no_configs and args.workload == "sweep" and not args.sizes:
+        del xin, host_in, host_out
+        out["configs"] = measure_configs(dev, stream, hbm_peak, plan_flags)
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(items, args, check=(plans, yout))
+        out["cpu_baseline"] = cpu_baseline(items, args, check=(plans, yout), uneven=uneven)
     return out
+
+
+REF_RUNNABLE = (2520, 59049, 117649, 1 << 20, 1009)
+FP64_PEAK_TFLOPS = 1.25     # nominal dense FP64 rate of a GB300 (no measured figure exists)
+
+
+def dominant_pass(plans_items, total_ms, hbm_peak):
+    """Roofline entry of the pass with the largest accumulated event time."""
+    best = None
+    for n, p in plans_items:
+        prof = p.profile_read()
+        for i, (tms, nl, bpl) in enumerate(prof):
+            if nl and (best is None or tms > best[0]):
+                best = (tms, nl, bpl, n, i, len(prof), p.describe()[i])
+        p.profile(False)
+    if not best:
+        return None
+    tms, nl, bpl, n, i, npass, pdesc = best
+    kind = "k_fast" if "kernel=fast" in pdesc else "k_pass"
+    shape = " ".join(w for w in pdesc.split() if w.startswith(("R=", "C=")))
+    avg_ms = tms / nl
+    achieved = bpl / (avg_ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+            "frac": round(achieved / hbm_peak, 3), "traffic": read_traffic(n, i),
+            "kernel": f"{kind} {shape} (N={n} pass {i + 1}/{npass}{', mid' if ' mid' in pdesc else ''})",
+            "bytes_per_launch": int(bpl), "avg_launch_ms": round(avg_ms, 4),
+            "share": round(tms / total_ms, 3) if total_ms > 0 else None}
+
+
+def measure_configs(dev: int, stream, hbm_peak: float, plan_flags: int, reps: int = 10):
+    """The other configurations, each timed on its own (events on the launching stream, inputs
+    resident, larger than L2 except C1's 33.5 MB, which is re-read from L2 between repetitions
+    unless flushed: C1 flushes L2 with a 256 MB write before every repetition)."""
+    import torch
+    import fyfft_gb300 as fg
+    res = {}
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+
+    def timed(fn, reps, flush_l2=False):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        tot = 0.0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(reps):
+            if flush_l2:
+                flush.zero_()
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / reps
+
+    def case(n, batch, dt, dist, seed, what="forward"):
+        npdt = np.complex64 if dt == "complex64" else np.complex128
+        esz = 8 if dt == "complex64" else 16
+        x = torch.empty(n * batch, dtype=torch.complex64 if dt == "complex64" else torch.complex128,
+                        device=f"cuda:{dev}")
+        fg.fill_random_device(seed, x, dist, stream)
+        y = torch.empty_like(x)
+        p = fg.FFT1D_C2C_invoker(n, dt, batch, flags=plan_flags)
+        if what == "forward":
+            fn = lambda: p.dispatch(False, x, y, stream)  # noqa: E731
+            nt = 1
+        else:
+            g = torch.empty_like(x)
+            fg.fill_random_device(3, g, "normal", stream)
+            gx = torch.empty_like(x)
+
+            def fn():
+                p.dispatch(False, x, y, stream)
+                p.adjoint(g, gx, 1.0, stream)
+            nt = 2
+        small = 2 * n * batch * esz < (128 << 20)
+        ms = timed(fn, reps, flush_l2=small)
+        p.profile(True)
+        fn()
+        torch.cuda.synchronize()
+        roof = dominant_pass([(n, p)], ms, hbm_peak)
+        gbs = nt * 2 * n * batch * esz / (ms * 1e-3) / 1e9
+        gfl = nt * flops(n) * batch / (ms * 1e-3) / 1e9
+        r = {"n": n, "batch": batch, "dtype": dt, "ms": round(ms, 4), "gflops": round(gfl, 1),
+             "gbs": round(gbs, 1), "hbm_frac": round(gbs / hbm_peak, 3), "passes": p.info()["passes"],
+             "conv_length": p.info()["conv_length"], "roofline": roof,
+             "l2": "flushed (256 MB write) before each repetition" if small else "inputs larger than L2"}
+        if dt == "complex128":
+            r["fp64_frac_of_nominal"] = round(gfl / (FP64_PEAK_TFLOPS * 1e3), 3)
+        del x, y
+        return r
+
+    res["c1"] = {"workload": "plain forward complex<double> N=4096 x 256, uniform[-1,1] seed 0",
+                 **case(4096, 256, "complex128", "uniform", 0)}
+    res["c4"] = {"workload": "forward + adjoint (F^H g), complex<float>, N(0,1) seed 3 / g seed 3",
+                 "cases": [case(1 << 20, 16, "complex64", "normal", 3, "grad"),
+                           case(100003, 32, "complex64", "normal", 3, "grad")]}
+    res["c5"] = {"workload": "large HBM-bound: complex<float> N=2^27 x 1 and 2^24 x 8, uniform[-1,1] seed 4",
+                 "cases": [case(1 << 27, 1, "complex64", "uniform", 4),
+                           case(1 << 24, 8, "complex64", "uniform", 4)]}
+    del flush
+    torch.cuda.empty_cache()
+    return res
 
 
 def uneven_batch(dev: int, stream, reps: int = 10, no_autotune: bool = False):
@@ -375,7 +482,9 @@ def uneven_batch(dev: int, stream, reps: int = 10, no_autotune: bool = False):
                 res["autotuned"] = {"stage_radix_cap": ent[0]["max_pass_radix"], "single_tile_kb": ent[0]["cols"],
                                     "tuner_ms": ent[0]["ms"]}
     res["speedup"] = round(res["plain_ms"] / res["batched_ms"], 2)
-    return res
+    b.execute(x, y, stream=stream)
+    torch.cuda.synchronize()
+    return res, (lengths, x.cpu().numpy(), y.cpu().numpy())
 
 
 def read_traffic(n: int, pass_index: int):
@@ -391,80 +500,157 @@ def read_traffic(n: int, pass_index: int):
 
 
 # ----------------------------------------------------------------------------------------------
-# CPU baseline (oracle port, FP64, all host threads, bounded sample)
+# The reference's own C++ FFT on the host cores (CPU baseline and the reference arm)
 # ----------------------------------------------------------------------------------------------
 
-def cpu_baseline(items, args, check=None):
+def cpu_model() -> str:
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return os.uname().machine
+
+
+def reference_handle():
+    """(oracle.Reference, None) when oracle/_ref/libfyref.so was built, else (None, why)."""
     from oracle import oracle as O
-    import fyfft_gb300 as fg
+    if not O.Reference.available():
+        return None, ("oracle/_ref/libfyref.so was not built: the reference's sources were not staged "
+                      "(oracle/ref/build_ref.sh needs the reference checkout once)")
+    return O.Reference(), None
+
+
+def reference_steps(items, steps: int, warmup: int, budget_s: float = 150.0):
+    """Times the reference's FFT1D_C2C_invoker over every item it can run, the whole batch per
+    step, one plan per host thread (oracle/ref/ref_capi.cpp pools).  Inputs come from the
+    oracle's restatement of the seeded generator, never from the GPU library.  Returns a dict
+    with the GFLOP/s, the timing details and the outputs of the last step."""
+    from oracle import oracle as O
+    ref, why = reference_handle()
+    if ref is None:
+        return {"unavailable": why}
     threads = os.cpu_count() or 1
-    tot_flops, tot_s, sample, errs = 0.0, 0.0, [], {}
-    for idx, (n, batch, dt, dist, seed) in enumerate(items):
-        cnt = min(batch, threads) if n < (1 << 24) else 1
-        npdt = np.complex64 if dt == "complex64" else np.complex128
-        x = fg.fill_random(seed, n * cnt, npdt, dist).reshape(cnt, n)
-        t = time.perf_counter()
-        y = O.fft_batch(x, inverse=False, threads=threads)
-        dt_s = time.perf_counter() - t
-        tot_flops += flops(n) * cnt
-        tot_s += dt_s
-        sample.append(f"{cnt}x{n}")
-        if check is not None:
-            plans, youts = check
-            g = youts[idx][: n * cnt].reshape(cnt, n).cpu().numpy()
-            errs[str(n)] = float(f"{O.rel_l2(g, y):.3e}")
-    res = {"value": round(tot_flops / tot_s / 1e9, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
-           "sample": "first transforms of each size (" + ", ".join(sample) + "), FP64 oracle restating the "
-                     "reference's radix/Rader/Bluestein algorithm, one transform per thread",
-           "seconds": round(tot_s, 2)}
-    if errs:
-        res["gpu_rel_l2_vs_fp64_oracle"] = errs
+    run, unsupported, pools, bufs = [], {}, [], []
+    plan_s = 0.0
+    for (n, batch, dt, dist, seed) in items:
+        if not ref.runnable(n):
+            unsupported[str(n)] = ("the reference falls back to its O(N^2) DFT (src/foye_FFT_dft.hpp), whose "
+                                   f"16 N^2-byte tables ({16 * n * n / 1e9:.0f} GB) cannot be allocated")
+            continue
+        x = O.fill_random(seed, n * batch, np.complex64, dist).reshape(batch, n)
+        y = np.empty_like(x)
+        pool = O.ReferencePool(ref, n, min(threads, batch))
+        plan_s += pool.plan_seconds
+        run.append((n, batch))
+        pools.append(pool)
+        bufs.append((x, y))
+    if not run:
+        return {"unavailable": "the reference can run none of this workload's lengths"}
+
+    def step():
+        return [pool.run(x, y) for pool, (x, y) in zip(pools, bufs)]
+    t = time.perf_counter()
+    step()
+    one = time.perf_counter() - t
+    steps = max(1, min(steps, int(budget_s / max(one, 1e-3))))
+    warm = max(0, min(warmup - 1, int(budget_s / max(one, 1e-3)) - steps))
+    for _ in range(warm):
+        step()
+    per = np.zeros(len(run))
+    t = time.perf_counter()
+    for _ in range(steps):
+        per += np.array(step())
+    el = time.perf_counter() - t
+    step_flops = sum(flops(n) * b for n, b in run)
+    for pool in pools:
+        pool.close()
+    return {"value": step_flops / (el / steps) / 1e9, "steps": steps, "warmup": warm + 1, "seconds": el,
+            "ms_per_step": el / steps * 1e3, "threads": threads, "run": run, "unsupported": unsupported,
+            "plan_s": plan_s, "build": ref.build_info(), "cpu": cpu_model(),
+            "per_size_gflops": {str(n): round(flops(n) * b * steps / per[i] / 1e9, 2) for i, (n, b) in enumerate(run)},
+            "outputs": {n: y for (n, _), (_, y) in zip(run, bufs)}}
+
+
+def reference_kind(build: str) -> str:
+    return ("reference's AVX2 C++ (FFT1D_C2C_invoker), native AVX2 build" if build.startswith("native")
+            else f"reference's AVX2 C++ (FFT1D_C2C_invoker), emulated on {cpu_model()} "
+                 f"(oracle/ref/portable_intrin.h, bit-identical to the native build on x86-64)")
+
+
+def cpu_baseline(items, args, check=None, uneven=None):
+    """The reference's own code on this host's cores (kind "reference"), a bounded run of the
+    same workload; where the GPU outputs are passed, their rel-L2 against the reference's
+    outputs and against the FP64 oracle (the checker)."""
+    from oracle import oracle as O
+    r = reference_steps(items, steps=3, warmup=1, budget_s=30.0)
+    if "unavailable" in r:
+        res = {"value": None, "unit": "GFLOP/s", "cores": os.cpu_count() or 1, "kind": "reference",
+               "unavailable": r["unavailable"]}
+    else:
+        res = {"value": round(r["value"], 3), "unit": "GFLOP/s", "cores": r["threads"], "kind": "reference",
+               "build": reference_kind(r["build"]),
+               "sample": (f"{r['steps']} step(s) of the whole batch of every length the reference runs "
+                          f"({', '.join(f'{b}x{n}' for n, b in r['run'])}), one plan per thread; "
+                          f"unsupported: {', '.join(r['unsupported']) or 'none'}"),
+               "seconds": round(r["seconds"], 2), "plan_s": round(r["plan_s"], 2),
+               "per_size_gflops": r["per_size_gflops"]}
+    if check is not None:
+        plans, youts = check
+        vs_ref, vs_oracle = {}, {}
+        threads = os.cpu_count() or 1
+        for (n, batch, dt, dist, seed), y in zip(items, youts):
+            g = y.view(batch, n)
+            rows = [0, batch - 1] if batch > 1 else [0]
+            gr = g[rows].cpu().numpy()
+            x = O.fill_random(seed, n * batch, np.complex128 if dt == "complex128" else np.complex64,
+                              dist).reshape(batch, n)
+            vs_oracle[str(n)] = float(f"{O.rel_l2(gr, O.fft_batch(x[rows].astype(np.complex128), threads=threads)):.3e}")
+            if "outputs" in r and n in r["outputs"]:
+                vs_ref[str(n)] = float(f"{O.rel_l2(g.cpu().numpy(), r['outputs'][n]):.3e}")
+        res["gpu_rel_l2_vs_reference"] = vs_ref
+        res["gpu_rel_l2_vs_fp64_oracle"] = vs_oracle
+        res["rel_l2_rows"] = "vs reference: whole batch; vs FP64 oracle: first and last transform"
+    if uneven is not None:
+        import concurrent.futures as cf
+        lengths, xh, yh = uneven
+        offs = np.concatenate([[0], np.cumsum(lengths)])
+
+        def err(i):
+            a, b = offs[i], offs[i + 1]
+            return O.rel_l2(yh[a:b], O.fft(xh[a:b]))
+        with cf.ThreadPoolExecutor(os.cpu_count() or 4) as ex:
+            errs = list(ex.map(err, range(len(lengths))))
+        res["mixed_batch_rel_l2_vs_fp64_oracle"] = {"max": float(f"{max(errs):.3e}"),
+                                                    "median": float(f"{statistics.median(errs):.3e}"),
+                                                    "transforms": len(errs)}
     return res
 
 
 def run_reference(args, rank: int, world: int):
+    """--impl reference: the reference's own FFT on the host cores, rank 0 only."""
     items, desc = workload(args.workload, args.sizes, args.batch)
     if rank != 0:
         return None
-    from oracle import oracle as O
-    import fyfft_gb300 as fg
-    threads = os.cpu_count() or 1
-    # bounded sample: per step, `threads` transforms of each size below 2^24 (one of larger ones)
-    xs = []
-    for (n, batch, dt, dist, seed) in items:
-        cnt = min(batch, threads) if n < (1 << 24) else 1
-        npdt = np.complex64 if dt == "complex64" else np.complex128
-        xs.append((n, fg.fill_random(seed, n * cnt, npdt, dist).reshape(cnt, n)))
-    step_flops = sum(flops(n) * x.shape[0] for n, x in xs)
-    # keep the whole run within a few minutes: time one step first, then cap the step count
-    def step():
-        for n, x in xs:
-            O.fft_batch(x, inverse=False, threads=threads)
-    t = time.perf_counter()
-    step()
-    one = time.perf_counter() - t
-    budget = 150.0
-    steps = max(1, min(args.steps, int(budget / max(one, 1e-3)) - args.warmup))
-    warm = min(args.warmup, max(0, int(budget / max(one, 1e-3)) - steps))
-    for _ in range(warm):
-        step()
-    t = time.perf_counter()
-    for _ in range(steps):
-        step()
-    el = time.perf_counter() - t
-    value = step_flops / (el / steps) / 1e9
-    sample = ", ".join(f"{x.shape[0]}x{n}" for n, x in xs)
+    r = reference_steps(items, args.steps, args.warmup)
+    if "unavailable" in r:
+        return {"impl": "reference", "unavailable": r["unavailable"]}
+    value = round(r["value"], 3)
+    sample = ", ".join(f"{b}x{n}" for n, b in r["run"])
     return {
-        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": world,
-        "steps": steps, "warmup": warm, "ms_per_step": round(el / steps * 1e3, 2), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64 (oracle port of the reference's algorithm)",
-        "data": "synthetic (seeded counter-based generator, fyg_fill_random)",
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world,
+        "steps": r["steps"], "warmup": r["warmup"], "ms_per_step": round(r["ms_per_step"], 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded counter-based generator, oracle restatement)",
         "config": {"workload": desc, "sizes": [it[0] for it in items], "batch": [it[1] for it in items],
-                   "sample_per_step": sample},
-        "cpu_baseline": {"value": round(value, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
-                         "sample": f"per step: {sample}; the reference's own AVX2 C++ is x86-only and "
-                                   f"does not build on this {os.uname().machine} host"},
-        "e2e": {"value": round(value, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                   "reference_runs": sample, "reference_unsupported": r["unsupported"],
+                   "value_over": "the lengths the reference runs (unsupported lengths excluded)"},
+        "cpu_baseline": {"value": value, "unit": "GFLOP/s", "cores": r["threads"], "kind": "reference",
+                         "build": reference_kind(r["build"]), "cpu": r["cpu"],
+                         "sample": f"per step the whole batch: {sample}; one plan per thread",
+                         "plan_s": round(r["plan_s"], 2), "per_size_gflops": r["per_size_gflops"]},
+        "e2e": {"value": value, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
 
@@ -484,6 +670,7 @@ def main():
                     help="autotune cache file; tuning is skipped when it already holds every size")
     ap.add_argument("--no-autotune", action="store_true", help="planner defaults instead of measured schedules")
     ap.add_argument("--no-uneven", action="store_true", help="skip the mixed-length batch comparison")
+    ap.add_argument("--no-configs", action="store_true", help="skip the C1 / C4 / C5 configuration lines")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 

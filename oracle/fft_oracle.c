@@ -476,3 +476,81 @@ int orc_fft_batch(size_t n, size_t batch, int inverse, const void* in, void* out
     free(th); free(jobs);
     return rc;
 }
+
+/* ------------------------------------------------------------------ */
+/* Seeded synthetic inputs                                             */
+/* ------------------------------------------------------------------ */
+/* The inputs of every configuration: element i of stream `seed` is a pure function of
+ * (seed, i), so that the GPU library's generator, this one and any number of threads produce
+ * the same values.  Bits: splitmix64 finalizer of seed + golden-ratio increments
+ * (2i for the real part, 2i+1 for the imaginary part).  uniform: 53-bit u -> 2u - 1;
+ * normal: Box-Muller, r = sqrt(-2 ln(1 - u1)), angle 2 pi u2.
+ * Restated here so that the CPU baseline and the fixtures never load the product library;
+ * tests/test_oracle_generator.py checks it equal to fyg_fill_random. */
+static uint64_t orc_mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static uint64_t orc_rand_bits(uint64_t seed, uint64_t i) {
+    const uint64_t phi = 0x9E3779B97F4A7C15ull;
+    return orc_mix64(orc_mix64(seed + phi) + (i + 1) * phi);
+}
+
+typedef struct {
+    uint64_t seed;
+    int dist, f32;
+    size_t lo, hi;
+    void* out;
+} fill_job;
+
+static void* fill_run(void* p) {
+    const fill_job* j = (const fill_job*)p;
+    for (size_t i = j->lo; i < j->hi; ++i) {
+        const double u1 = (double)(orc_rand_bits(j->seed, 2 * i) >> 11) * 0x1.0p-53;
+        const double u2 = (double)(orc_rand_bits(j->seed, 2 * i + 1) >> 11) * 0x1.0p-53;
+        double re, im;
+        if (j->dist == 0) {
+            re = 2.0 * u1 - 1.0;
+            im = 2.0 * u2 - 1.0;
+        } else {
+            const double r = sqrt(-2.0 * log(1.0 - u1));
+            re = r * cos(6.283185307179586 * u2);
+            im = r * sin(6.283185307179586 * u2);
+        }
+        if (j->f32) {
+            ((float*)j->out)[2 * i] = (float)re;
+            ((float*)j->out)[2 * i + 1] = (float)im;
+        } else {
+            ((double*)j->out)[2 * i] = re;
+            ((double*)j->out)[2 * i + 1] = im;
+        }
+    }
+    return NULL;
+}
+
+/* dist: 0 uniform[-1, 1), 1 normal; f32: 1 complex<float>, 0 complex<double> */
+int orc_fill_random(uint64_t seed, int dist, int f32, size_t n, void* out, int threads) {
+    if (threads < 1) threads = 1;
+    if (threads > 64) threads = 64;
+    if (n < ((size_t)1 << 16)) threads = 1;
+    pthread_t th[64];
+    fill_job jobs[64];
+    for (int t = 0; t < threads; ++t) {
+        jobs[t].seed = seed;
+        jobs[t].dist = dist;
+        jobs[t].f32 = f32;
+        jobs[t].lo = n * (size_t)t / (size_t)threads;
+        jobs[t].hi = n * (size_t)(t + 1) / (size_t)threads;
+        jobs[t].out = out;
+    }
+    int started[64] = {0};
+    for (int t = 1; t < threads; ++t) started[t] = pthread_create(&th[t], NULL, fill_run, &jobs[t]) == 0;
+    fill_run(&jobs[0]);
+    for (int t = 1; t < threads; ++t) {
+        if (started[t]) pthread_join(th[t], NULL);
+        else fill_run(&jobs[t]);   /* no thread: this range on the calling thread */
+    }
+    return 0;
+}

@@ -6,8 +6,10 @@ CPU baseline; the GPU library never does.
 
 ``fft`` / ``dft`` restate the reference's transform (foye_FFT.hpp:128-151: forward
 exp(-2 pi i kn/N), inverse exp(+2 pi i kn/N) scaled by 1/N) in FP64 with long-double
-twiddles.  ``Reference`` wraps the reference's own C++ code when oracle/_ref/libfyref.so was
-built (x86-64 hosts only, oracle/ref/build_ref.sh).
+twiddles.  ``fill_random`` generates the seeded inputs of every configuration without the GPU
+library.  ``Reference`` wraps the reference's own C++ code when oracle/_ref/libfyref.so was
+built by oracle/ref/build_ref.sh (natively with AVX2 on x86-64; elsewhere against the
+portable intrinsics of oracle/ref/portable_intrin.h).
 """
 from __future__ import annotations
 
@@ -53,6 +55,8 @@ def lib() -> ctypes.CDLL:
         L.orc_dft.argtypes = [sz, i, vp, vp]
         L.orc_dft_sampled.argtypes = [sz, i, vp, vp, sz, vp]
         L.orc_fft_batch.argtypes = [sz, sz, i, vp, vp, i, i]
+        L.orc_fill_random.argtypes = [ctypes.c_uint64, i, i, sz, vp, i]
+        L.orc_fill_random.restype = i
         for f in (L.orc_fft, L.orc_dft, L.orc_dft_sampled, L.orc_fft_batch):
             f.restype = i
         _lib = L
@@ -127,6 +131,22 @@ def dft_sampled(x, idx, inverse: bool = False) -> np.ndarray:
     return out
 
 
+def fill_random(seed: int, n: int, dtype=np.complex64, dist: str = "normal", threads: int | None = None) -> np.ndarray:
+    """n seeded complex values (dist "uniform": re, im in [-1, 1); "normal": N(0, 1) each),
+    identical to the GPU library's fyg_fill_random for the same (seed, dist, dtype)."""
+    dtype = np.dtype(dtype)
+    if dtype not in (np.complex64, np.complex128):
+        raise ValueError("dtype must be complex64 or complex128")
+    if dist not in ("uniform", "normal"):
+        raise ValueError("dist must be 'uniform' or 'normal'")
+    out = np.empty(int(n), dtype=dtype)
+    rc = lib().orc_fill_random(int(seed), 0 if dist == "uniform" else 1, int(dtype == np.complex64), int(n),
+                               out.ctypes.data, int(threads or os.cpu_count() or 1))
+    if rc:
+        raise RuntimeError("orc_fill_random failed")
+    return out
+
+
 def rel_l2(a, b) -> float:
     a = np.asarray(a, dtype=np.complex128)
     b = np.asarray(b, dtype=np.complex128)
@@ -150,7 +170,17 @@ class Reference:
         L.fyref_plan_execute.argtypes = [vp, i, vp, vp]
         L.fyref_batch.argtypes = [sz, sz, i, vp, vp, i, ctypes.POINTER(ctypes.c_double),
                                   ctypes.POINTER(ctypes.c_double)]
+        L.fyref_pool_create.argtypes = [sz, i, ctypes.POINTER(ctypes.c_double)]
+        L.fyref_pool_create.restype = vp
+        L.fyref_pool_run.argtypes = [vp, sz, i, vp, vp, ctypes.POINTER(ctypes.c_double)]
+        L.fyref_pool_destroy.argtypes = [vp]
+        L.fyref_build_info.restype = ctypes.c_char_p
         self.L = L
+        self.path = path
+
+    def build_info(self) -> str:
+        """'native x86_64', 'emulated aarch64' or 'emulated x86_64'."""
+        return self.L.fyref_build_info().decode()
 
     @staticmethod
     def available(path: str = REF_PATH) -> bool:
@@ -182,3 +212,36 @@ class Reference:
                               ctypes.byref(t), ctypes.byref(tp)):
             raise RuntimeError(f"reference cannot run length {n}")
         return y, t.value, tp.value
+
+
+class ReferencePool:
+    """`threads` worker threads with one reference plan of length n each (plans hold mutable
+    workspace and are never shared); ``run`` splits a contiguous batch over them."""
+
+    def __init__(self, ref: Reference, n: int, threads: int):
+        t = ctypes.c_double()
+        self.ref, self.n = ref, int(n)
+        self.h = ref.L.fyref_pool_create(self.n, int(threads), ctypes.byref(t))
+        if not self.h:
+            raise RuntimeError(f"reference cannot run length {n}")
+        self.plan_seconds = t.value
+
+    def run(self, x: np.ndarray, y: np.ndarray, inverse: bool = False) -> float:
+        """y = transform of x ((batch, n) complex64, C-contiguous); returns the wall seconds."""
+        assert x.dtype == np.complex64 and y.dtype == np.complex64 and x.flags.c_contiguous and y.flags.c_contiguous
+        assert x.shape[-1] == self.n and x.size == y.size
+        t = ctypes.c_double()
+        self.ref.L.fyref_pool_run(self.h, x.size // self.n, int(inverse), x.ctypes.data, y.ctypes.data,
+                                  ctypes.byref(t))
+        return t.value
+
+    def close(self):
+        if self.h:
+            self.ref.L.fyref_pool_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

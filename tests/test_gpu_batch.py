@@ -114,3 +114,28 @@ def test_batch_autotune_caches_a_choice_and_the_tuned_batch_is_exact(tmp_path):
     torch.cuda.synchronize()
     for n, xi, yi in zip(lengths, split(x, lengths), split(y.cpu().numpy(), lengths)):
         assert O.rel_l2(yi, O.fft(xi)) <= 2e-6, n
+
+
+def test_full_mixed_length_configuration_vs_oracle():
+    """The benchmark's own batch: all 4096 lengths (seed 2, 0.70 7-smooth / 0.15 prime / 0.15
+    other) in one persistent launch, every transform within 2e-6 (and 4 log2 N eps32) of the
+    FP64 oracle."""
+    import concurrent.futures as cf
+    import os
+    lengths = uneven_lengths(4096, 2)
+    b = fg.UnevenBatch(lengths)
+    x = fg.fill_random(2, sum(lengths), np.complex64, "uniform")
+    xd = torch.from_numpy(x).cuda()
+    y = torch.empty_like(xd)
+    b.execute(xd, y)
+    assert b.status() == 0
+    ys = split(y.cpu().numpy(), lengths)
+    xs = split(x, lengths)
+
+    def err(i):
+        return O.rel_l2(ys[i], O.fft(xs[i]))
+    with cf.ThreadPoolExecutor(os.cpu_count() or 4) as ex:
+        errs = list(ex.map(err, range(len(lengths))))
+    worst = max(range(len(lengths)), key=lambda i: errs[i])
+    assert errs[worst] <= 2e-6, (lengths[worst], errs[worst])
+    assert all(e <= 4 * np.log2(n) * float(np.finfo(np.float32).eps) for e, n in zip(errs, lengths))

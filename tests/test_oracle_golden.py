@@ -76,3 +76,41 @@ def test_reference_batch_threads_if_built():
     y, t, _ = ref.batch(x, threads=2)
     assert t > 0
     assert O.rel_l2(y, O.fft(x)) < 4 * 10 * EPS32
+
+
+CONFIG = os.path.join(os.path.dirname(__file__), "golden", "config_vectors.npz")
+
+
+@pytest.fixture(scope="module")
+def config_golden():
+    return np.load(CONFIG)
+
+
+def config_case(g, key):
+    n, batch = int(g[f"{key}_n"]), int(g[f"{key}_batch"])
+    x = O.fill_random(int(g[f"{key}_seed"]), n * batch, np.complex64, str(g[f"{key}_dist"])).reshape(batch, n)
+    return n, x
+
+
+def test_config_inputs_come_from_the_seeded_generator(config_golden):
+    for key in config_golden["keys"]:
+        key = str(key)
+        n, batch = int(config_golden[f"{key}_n"]), int(config_golden[f"{key}_batch"])
+        head = O.fill_random(int(config_golden[f"{key}_seed"]), 8, np.complex64, str(config_golden[f"{key}_dist"]))
+        assert np.array_equal(head, config_golden[f"{key}_head"]), key
+
+
+# the 2^27 transform takes about a minute in the FP64 oracle; its GPU output is compared with
+# the reference's directly in tests/test_gpu_reference_parity.py
+@pytest.mark.parametrize("key", ["c1", "c2_2520", "c2_59049", "c2_117649", "c2_1048576", "c2_1009", "c4",
+                                 "c5_16777216"])
+def test_oracle_matches_reference_on_config_inputs(config_golden, key):
+    g = config_golden
+    n, x = config_case(g, key)
+    rows, idx = g[f"{key}_rows"], g[f"{key}_idx"]
+    inverse = bool(int(g[f"{key}_inverse"]))
+    y = O.fft_batch(x[rows].astype(np.complex128), inverse=inverse, threads=os.cpu_count() or 1)
+    if inverse:
+        y = y * n        # the reference gradient n * IFFT(g)
+    err = O.rel_l2(y[:, idx], g[f"{key}_out"])
+    assert err <= 4 * np.log2(n) * EPS32, (key, err)
