@@ -18,8 +18,10 @@ with its dominant pass's roofline), the mixed-length batch in one persistent lau
 launch sequence per plan (batched_vs_plain), and the CPU baseline with the GPU's rel-L2 against
 the reference and the FP64 oracle.
 
-N > 1 runs one independent replica per GPU (the path does not shard): value is the total
-over ranks divided by the max time over ranks.  --impl reference times the reference's own
+N > 1 (torchrun, one rank per GPU) shards a global batch of batch x N transforms per length
+with the library's partition (fyg_partition): each rank runs its contiguous shard of the
+seeded stream, no collective on the data path; value is the units all ranks processed divided
+by the max time over ranks (weak scaling).  --impl reference times the reference's own
 C++ FFT (oracle/_ref/libfyref.so: the unmodified reference, built natively with AVX2 on x86-64
 and against oracle/ref/portable_intrin.h on the aarch64 GPU hosts) on all host cores, one plan
 per thread, over the whole batch of every workload length it can run.
@@ -160,11 +162,19 @@ def run_ours(args, rank: int, world: int):
                 fg.autotune(n, dt, batch, cache_path=cache)
     plan_flags = 0 if args.no_autotune else fg.FYG_FLAG_AUTOTUNED
 
+    # N > 1: the global batch of every length is batch x N transforms, sharded by the library's
+    # partition (fyg_partition); this rank runs its contiguous shard of the seeded stream, so
+    # per-GPU work stays fixed as N grows (weak scaling) and no rank repeats another's work
+    shards = []
+    for i, (n, batch, dt, dist, seed) in enumerate(items):
+        b = fg.partition(batch * world, world)
+        shards.append(b[rank])
+        items[i] = (n, b[rank + 1] - b[rank], dt, dist, seed)
     plans, xin, yout, host_in, host_out = [], [], [], [], []
-    for (n, batch, dt, dist, seed) in items:
+    for (n, batch, dt, dist, seed), first in zip(items, shards):
         npdt = np.complex64 if dt == "complex64" else np.complex128
         tdt = torch.complex64 if dt == "complex64" else torch.complex128
-        x = fg.fill_random(seed, n * batch, npdt, dist)
+        x = fg.fill_random(seed, n * batch, npdt, dist, first=first * n)
         hx = torch.from_numpy(x).pin_memory()
         host_in.append(hx)
         host_out.append(torch.empty_like(hx).pin_memory())
@@ -295,7 +305,8 @@ def run_ours(args, rank: int, world: int):
         "data": "synthetic (seeded counter-based generator, fyg_fill_random)",
         "config": {"workload": desc, "sizes": [it[0] for it in items], "batch": [it[1] for it in items],
                    "l2": f"inputs larger than L2 ({in_bytes / 1e9:.2f} GB per step), no flush",
-                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "parallelism": (f"batch sharded over {world} GPUs (fyg_partition, no collective; "
+                                   f"global batch = per-GPU batch x {world})") if world > 1 else "single GPU",
                    "schedules": "planner defaults" if args.no_autotune else
                    "autotuned on this device before timing (fyg_autotune; conv length, pass radix, cols)"},
         "gbs": round(step_bytes * world / (ms_step * 1e-3) / 1e9, 1),
@@ -324,7 +335,8 @@ def run_ours(args, rank: int, world: int):
             "ms_per_step": round(sub_ms, 4), "from": "per_size device times (events, 5 repetitions each)"}
     uneven = None
     if not args.no_uneven:
-        out["batched_vs_plain"], uneven = uneven_batch(dev, stream, no_autotune=args.no_autotune)
+        out["batched_vs_plain"], uneven = uneven_batch(dev, stream, no_autotune=args.no_autotune, rank=rank,
+                                                       world=world)
     if not args.no_configs and args.workload == "sweep" and not args.sizes:
         del xin, host_in, host_out
         out["configs"] = measure_configs(dev, stream, hbm_peak, plan_flags)
@@ -435,13 +447,17 @@ def measure_configs(dev: int, stream, hbm_peak: float, plan_flags: int, reps: in
     return res
 
 
-def uneven_batch(dev: int, stream, reps: int = 10, no_autotune: bool = False):
+def uneven_batch(dev: int, stream, reps: int = 10, no_autotune: bool = False, rank: int = 0, world: int = 1):
     """The mixed-length batch (4096 lengths in [16, 65536], 7-smooth / prime / other, seed 2):
-    one persistent launch (CUDA graph) against one launch sequence per transform."""
+    one persistent launch (CUDA graph) against one launch sequence per transform.  With N > 1
+    ranks each runs its cost-balanced contiguous shard of the 4096 (fyg_partition)."""
     import torch
     import fyfft_gb300 as fg
     from fyfft_gb300.workloads import uneven_lengths
     lengths = uneven_lengths(4096, 2)
+    bounds = fg.partition(lengths, world)
+    first = int(sum(lengths[:bounds[rank]]))
+    lengths = lengths[bounds[rank]:bounds[rank + 1]]
     t0 = time.perf_counter()
     tuned = None
     if not no_autotune:
@@ -451,7 +467,7 @@ def uneven_batch(dev: int, stream, reps: int = 10, no_autotune: bool = False):
     t1 = time.perf_counter()
     b = fg.UnevenBatch(lengths, flags=0 if no_autotune else fg.FYG_FLAG_AUTOTUNED)
     create_s = time.perf_counter() - t1
-    x = torch.from_numpy(fg.fill_random(2, sum(lengths), np.complex64, "uniform")).to(f"cuda:{dev}")
+    x = torch.from_numpy(fg.fill_random(2, sum(lengths), np.complex64, "uniform", first=first)).to(f"cuda:{dev}")
     y = torch.empty_like(x)
     fl = sum(flops(n) for n in lengths)
     res = {"workload": "4096 complex<float> transforms, lengths log-uniform in [16, 65536] "

@@ -39,7 +39,9 @@ EXPORTED_SYMBOLS = (
     "fyg_batch_execute", "fyg_batch_execute_plain", "fyg_batch_status", "fyg_batch_inject_stall",
     "fyg_execute_noalloc", "fyg_last_error_string",
     "fyg_fill_random",
-    "fyg_fill_random_device", "fyg_version",
+    "fyg_fill_random_device", "fyg_version", "fyg_plan_cache_stats", "fyg_plan_cache_clear",
+    "fyg_partition", "fyg_multi_create", "fyg_multi_shards", "fyg_multi_execute", "fyg_multi_execute_device",
+    "fyg_multi_synchronize", "fyg_multi_destroy", "fyg_fill_random_at", "fyg_fill_random_device_at",
 )
 
 
@@ -95,7 +97,18 @@ def lib() -> ctypes.CDLL:
         L.fyg_last_error_string.restype = ctypes.c_char_p
         L.fyg_fill_random.argtypes = [u64, i, i, sz, vp]
         L.fyg_fill_random_device.argtypes = [u64, i, i, sz, vp, vp]
+        L.fyg_fill_random_at.argtypes = [u64, i, i, sz, sz, vp]
+        L.fyg_fill_random_device_at.argtypes = [u64, i, i, sz, sz, vp, vp]
         L.fyg_version.restype = ctypes.c_char_p
+        L.fyg_plan_cache_stats.argtypes = [ctypes.POINTER(sz), ctypes.POINTER(sz), ctypes.POINTER(u64),
+                                           ctypes.POINTER(u64)]
+        L.fyg_partition.argtypes = [ctypes.POINTER(sz), sz, i, ctypes.POINTER(sz)]
+        L.fyg_multi_create.argtypes = [sz, i, sz, i, ctypes.POINTER(i), i, ctypes.POINTER(vp)]
+        L.fyg_multi_shards.argtypes = [vp, ctypes.POINTER(i), ctypes.POINTER(sz)]
+        L.fyg_multi_execute.argtypes = [vp, vp, vp, i]
+        L.fyg_multi_execute_device.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), i]
+        L.fyg_multi_synchronize.argtypes = [vp]
+        L.fyg_multi_destroy.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -122,6 +135,18 @@ def autotune_batch(lengths, dtype="complex64", cache_path: str | None = None) ->
     path = cache_path.encode() if cache_path else None
     check(lib().fyg_batch_autotune(arr, len(lens), code, path, ctypes.byref(ms)))
     return ms.value
+
+
+def plan_cache_stats() -> dict:
+    """Entries and device bytes of the process-wide table cache, and its hit / miss counts."""
+    e, b, h, m = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_uint64(), ctypes.c_uint64()
+    check(lib().fyg_plan_cache_stats(ctypes.byref(e), ctypes.byref(b), ctypes.byref(h), ctypes.byref(m)))
+    return {"entries": e.value, "bytes": b.value, "hits": h.value, "misses": m.value}
+
+
+def plan_cache_clear() -> None:
+    """Free the cached tables that no live plan uses."""
+    check(lib().fyg_plan_cache_clear())
 
 
 def check(rc: int) -> None:
@@ -165,19 +190,20 @@ def _buffer_ptr(x):
     return x.data_ptr(), x.numel() // dt[1], dt[0], x.is_cuda
 
 
-def fill_random(seed: int, n_complex: int, dtype=np.complex64, dist: str = "uniform") -> np.ndarray:
-    """Seeded synthetic data on the host (uniform re/im in [-1, 1) or standard normal)."""
+def fill_random(seed: int, n_complex: int, dtype=np.complex64, dist: str = "uniform", first: int = 0) -> np.ndarray:
+    """Seeded synthetic data on the host (uniform re/im in [-1, 1) or standard normal):
+    elements [first, first + n_complex) of stream `seed`."""
     out = np.empty(n_complex, dtype=dtype)
     code = FYG_C32 if np.dtype(dtype) == np.complex64 else FYG_C64
-    check(lib().fyg_fill_random(seed, 0 if dist == "uniform" else 1, code, n_complex, out.ctypes.data))
+    check(lib().fyg_fill_random_at(seed, 0 if dist == "uniform" else 1, code, int(first), n_complex, out.ctypes.data))
     return out
 
 
-def fill_random_device(seed: int, out, dist: str = "uniform", stream=None) -> None:
+def fill_random_device(seed: int, out, dist: str = "uniform", stream=None, first: int = 0) -> None:
     """Same stream as fill_random, generated on the GPU into a CUDA tensor."""
     ptr, n, code, _ = _buffer_ptr(out)
-    check(lib().fyg_fill_random_device(seed, 0 if dist == "uniform" else 1, code, n, ptr,
-                                       _stream_handle(stream)))
+    check(lib().fyg_fill_random_device_at(seed, 0 if dist == "uniform" else 1, code, int(first), n, ptr,
+                                          _stream_handle(stream)))
 
 
 class FFT1D_C2C_invoker:
@@ -334,6 +360,65 @@ class UnevenBatch:
         py, _, _, _ = _buffer_ptr(y)
         check(lib().fyg_batch_execute_plain(self._h, px, py, FYG_INVERSE if invert else FYG_FORWARD,
                                             _stream_handle(stream)))
+
+
+def partition(batch, parts: int) -> list[int]:
+    """Contiguous shards of near-equal cost: bounds[0..parts] (fyg_partition).  `batch` is a
+    count (uniform batch) or a sequence of transform lengths (cost n log2 n each)."""
+    bounds = (ctypes.c_size_t * (parts + 1))()
+    if isinstance(batch, int):
+        check(lib().fyg_partition(None, batch, int(parts), bounds))
+    else:
+        lens = [int(n) for n in batch]
+        arr = (ctypes.c_size_t * max(len(lens), 1))(*lens)
+        check(lib().fyg_partition(arr, len(lens), int(parts), bounds))
+    return list(bounds)
+
+
+class MultiDevicePlan:
+    """`batch` transforms of length N sharded over `devices` (a device may repeat): one plan and
+    stream per shard, no collective (fyg_multi_*)."""
+
+    def __init__(self, length: int, dtype="complex64", batch: int = 1, devices=(0,), flags: int = 0):
+        self.N, self.batch = int(length), int(batch)
+        self.dtype_code = FYG_C32 if str(dtype).endswith("complex64") else FYG_C64
+        devs = (ctypes.c_int * len(devices))(*[int(d) for d in devices])
+        h = ctypes.c_void_p()
+        check(lib().fyg_multi_create(self.N, self.dtype_code, self.batch, flags, devs, len(devices), ctypes.byref(h)))
+        self._h = h
+        nd = ctypes.c_int()
+        b = (ctypes.c_size_t * (len(devices) + 1))()
+        check(lib().fyg_multi_shards(h, ctypes.byref(nd), b))
+        self.devices = list(devices)
+        self.bounds = list(b)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fyg_multi_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def execute(self, x: np.ndarray, y: np.ndarray, invert: bool = False) -> None:
+        """Host arrays holding the whole batch; returns when y is complete."""
+        px, nx, dx, _ = _buffer_ptr(x)
+        py, ny, dy, _ = _buffer_ptr(y)
+        if dx != self.dtype_code or dy != self.dtype_code or nx < self.N * self.batch or ny < self.N * self.batch:
+            raise ValueError("buffers do not match the plan")
+        check(lib().fyg_multi_execute(self._h, px, py, FYG_INVERSE if invert else FYG_FORWARD))
+
+    def execute_device(self, xs, ys, invert: bool = False) -> None:
+        """Per-shard device tensors (shard i on devices[i]); asynchronous."""
+        ins = (ctypes.c_void_p * len(xs))(*[_buffer_ptr(t)[0] for t in xs])
+        outs = (ctypes.c_void_p * len(ys))(*[_buffer_ptr(t)[0] for t in ys])
+        check(lib().fyg_multi_execute_device(self._h, ins, outs, FYG_INVERSE if invert else FYG_FORWARD))
+
+    def synchronize(self) -> None:
+        check(lib().fyg_multi_synchronize(self._h))
 
 
 _plan_cache: dict = {}

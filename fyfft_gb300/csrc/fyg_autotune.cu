@@ -1,7 +1,9 @@
 // fyg_autotune.cu -- measured choice of a length's schedule, cached in a JSON file.
 //
 // For one length the candidates are the knobs the planner otherwise sets by rule:
-//   single-pass lengths   transforms per CTA (C), i.e. threads per transform = threads / C
+//   single-pass lengths   transforms per CTA (C) and the thread policy (about 16 points per
+//                         thread, or one thread per butterfly of the widest stage), i.e. the
+//                         threads per transform
 //   multi-pass lengths    a cap on the pass radix (more, smaller passes or fewer, larger ones)
 //   Rader / Bluestein     the convolution length (7-smooth lengths up to 8% above the minimum,
 //                         and for Bluestein the power of two), a cap on its pass radix and the
@@ -73,16 +75,19 @@ void load(const std::string& path) {
         }
         char key[64];
         unsigned long long r = 0, m = 0;
-        int c = 0, o = 0;
+        int c = 0, o = 0, th = 0;
         double ms = 0;
-        if (std::sscanf(line.c_str(),
-                        " \"%63[^\"]\": {\"max_pass_radix\": %llu, \"conv_length\": %llu, \"cols\": %d, \"order\": %d, \"ms\": %lf",
-                        key, &r, &m, &c, &o, &ms) == 6) {
+        const int got = std::sscanf(
+            line.c_str(),
+            " \"%63[^\"]\": {\"max_pass_radix\": %llu, \"conv_length\": %llu, \"cols\": %d, \"order\": %d, \"threads\": %d, \"ms\": %lf",
+            key, &r, &m, &c, &o, &th, &ms);
+        if (got == 7) {
             TuneChoice t;
             t.max_pass_radix = r;
             t.conv_length = m;
             t.cols = c;
             t.order = o;
+            t.threads = th;
             t.ms = ms;
             g_cache.entries[key] = t;
         }
@@ -98,12 +103,13 @@ int save() {
     f << "{\n  \"device\": \"" << g_cache.device << "\",\n  \"entries\": {\n";
     size_t i = 0;
     for (auto& kv : g_cache.entries) {
-        char buf[256];
+        char buf[320];
         std::snprintf(buf, sizeof(buf),
-                      "    \"%s\": {\"max_pass_radix\": %llu, \"conv_length\": %llu, \"cols\": %d, \"order\": %d, \"ms\": %.6f}%s\n",
+                      "    \"%s\": {\"max_pass_radix\": %llu, \"conv_length\": %llu, \"cols\": %d, \"order\": %d, "
+                      "\"threads\": %d, \"ms\": %.6f}%s\n",
                       kv.first.c_str(), (unsigned long long)kv.second.max_pass_radix,
-                      (unsigned long long)kv.second.conv_length, kv.second.cols, kv.second.order, kv.second.ms,
-                      ++i < g_cache.entries.size() ? "," : "");
+                      (unsigned long long)kv.second.conv_length, kv.second.cols, kv.second.order, kv.second.threads,
+                      kv.second.ms, ++i < g_cache.entries.size() ? "," : "");
         f << buf;
     }
     f << "  }\n}\n";
@@ -134,18 +140,24 @@ std::vector<TuneChoice> candidates(size_t n, int dtype, size_t batch) {
     const int cb = dtype == FYG_C32 ? 8 : 16;
     std::vector<TuneChoice> out;
     out.push_back(TuneChoice());
-    auto add = [&](uint64_t r, uint64_t m, int c, int o = 0) {
+    auto add = [&](uint64_t r, uint64_t m, int c, int o = 0, int th = 0) {
         TuneChoice t;
         t.max_pass_radix = r;
         t.conv_length = m;
         t.cols = c;
         t.order = o;
+        t.threads = th;
         out.push_back(t);
     };
+    // single-pass lengths: transforms per CTA x thread policy (threads per transform)
+    auto add_single = [&](uint64_t m, uint64_t L) {
+        for (int c : {1, 2, 4, 8, 16, 32, 64})
+            if ((size_t)c <= batch && (uint64_t)c * L <= 16384)
+                for (int th : {0, 1}) add(0, m, c, 0, th);
+    };
     if (smooth(n, 13)) {
-        if (n <= 16384 && tile_fits(cb, (int)n, 1, true)) {
-            for (int c : {1, 2, 4, 8, 16, 32, 64})
-                if ((size_t)c <= batch && (uint64_t)c * n <= 16384) add(0, 0, c);
+        if (single_pass_fits(cb, n, (size_t)-1)) {
+            add_single(0, n);
         } else {
             for (uint64_t r : {2048ull, 1024ull, 512ull, 256ull, 128ull}) add(r, 0, 0);
             add(0, 0, 0, 1);
@@ -161,9 +173,14 @@ std::vector<TuneChoice> candidates(size_t n, int dtype, size_t batch) {
         while (m2 < 2 * n - 1) m2 <<= 1;
         if (std::find(ms.begin(), ms.end(), m2) == ms.end()) ms.push_back(m2);
     }
-    for (uint64_t m : ms)
+    for (uint64_t m : ms) {
+        if (single_pass_fits(cb, m, (size_t)-1)) {
+            add_single(m, m);
+            continue;
+        }
         for (uint64_t r : {0ull, 256ull})
             for (int o : {0, 1}) add(r, m, 0, o);
+    }
     return out;
 }
 
@@ -218,7 +235,8 @@ extern "C" int fyg_autotune(size_t n, int dtype, size_t batch, const char* cache
     const bool verbose = std::getenv("FYG_AUTOTUNE_VERBOSE") != nullptr;
     for (const TuneChoice& c : candidates(n, dtype, batch)) {
         fyg_plan* pl = nullptr;
-        if (plan_create_opts(n, dtype, batch, 0, c.max_pass_radix, c.conv_length, c.cols, c.order, &pl) != FYG_OK)
+        if (plan_create_opts(n, dtype, batch, 0, c.max_pass_radix, c.conv_length, c.cols, c.order, c.threads, &pl) !=
+            FYG_OK)
             continue;
         double t = 1e30;
         bool ok = fyg_execute(pl, in.ptr, out.ptr, FYG_FORWARD, nullptr) == FYG_OK;
@@ -233,9 +251,10 @@ extern "C" int fyg_autotune(size_t n, int dtype, size_t batch, const char* cache
         }
         fyg_plan_destroy(pl);
         if (verbose)
-            std::fprintf(stderr, "fyg_autotune n=%zu max_pass_radix=%llu conv_length=%llu cols=%d order=%d: %s %.4f ms\n", n,
-                         (unsigned long long)c.max_pass_radix, (unsigned long long)c.conv_length, c.cols, c.order,
-                         ok ? "ok" : "failed", ok ? t : 0.0);
+            std::fprintf(stderr,
+                         "fyg_autotune n=%zu max_pass_radix=%llu conv_length=%llu cols=%d order=%d threads=%d: %s %.4f ms\n",
+                         n, (unsigned long long)c.max_pass_radix, (unsigned long long)c.conv_length, c.cols, c.order,
+                         c.threads, ok ? "ok" : "failed", ok ? t : 0.0);
         if (ok && (!have || t < best.ms)) {
             best = c;
             best.ms = t;

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <memory>
 #include <map>
 #include <string>
@@ -11,13 +12,15 @@
 #include "../../include/fygpu.h"
 #include "fyg_internal.h"
 
+struct fyg_plan;
+
 namespace fyg {
 
 int set_error(int code, const std::string& msg);
 void clear_error();
 const char* last_error();
 int cuda_error(cudaError_t e, const char* what);
-void fill_random_host(uint64_t seed, int dist, int dtype, size_t n, void* out);
+void fill_random_host(uint64_t seed, int dist, int dtype, size_t first, size_t n, void* out);
 
 FastDiv make_fastdiv(uint32_t d);
 
@@ -32,6 +35,9 @@ size_t smem_for(int cb, int R, int C, bool colmajor);
 int tile_class(int cb, int rmax);
 int pick_variant(int compute_cb, int tin_cb, int tout_cb, int cls);
 int threads_for(int R, int C, int maxt);
+int single_pass_cols(int cb, int L, size_t batch, int requested);
+int single_pass_threads(int L, int C, const std::vector<int>& rad, int requested);
+bool single_pass_fits(int cb, uint64_t n, size_t cap);
 void twiddle_ld(uint64_t t, uint64_t n, long double* c, long double* s);
 std::vector<unsigned char> host_local_table(int R, int cb);
 
@@ -40,6 +46,7 @@ struct TuneChoice {
     uint64_t max_pass_radix = 0, conv_length = 0;
     int cols = 0;
     int order = 0;       // 1: reversed pass order (the fused mid pass takes the other radix)
+    int threads = 0;     // single-pass thread policy (single_pass_threads)
     double ms = 0;
 };
 bool tune_lookup(size_t n, int dtype, TuneChoice* out);
@@ -49,7 +56,7 @@ int tune_store_key(const std::string& key, const TuneChoice& choice, const char*
 // Options of uneven-batch group plans for plans created next on this thread (0 = defaults).
 void set_batch_tile_options(int radix_cap, size_t single_cap_bytes);
 int plan_create_opts(size_t n, int dtype, size_t batch, int flags, uint64_t max_pass_radix, uint64_t conv_length,
-                     int cols, int order, fyg_plan** out);
+                     int cols, int order, int threads, fyg_plan** out);
 // Layout of the user buffers of plans created next on this thread (0 = contiguous).
 void set_plan_layout(size_t idist, size_t odist);
 void host_two_level(uint64_t L, int cb, std::vector<unsigned char>& hi, std::vector<unsigned char>& lo, int* shift);
@@ -87,18 +94,12 @@ struct PassDesc {
     int64_t in_elem_bytes, out_elem_bytes;
 };
 
-// In-CTA schedule of a length-R sub-transform.
-struct TilePlan {
-    int R = 0;
-    std::vector<int> radix;
-};
-
-// Per-length tables (w_R for the in-CTA stages; two-level w_L for inter-pass twiddles).
-struct TwiddleSet {
-    DevBuf local_f, local_d;   // keyed per R inside the plan
-};
-
-struct fyg_plan_impl;
+// Process-wide cache of read-only plan tables (twiddles, chirps, Rader index maps, convolution
+// spectra, thread-order tables), keyed by device and content.  A plan holds shared references
+// to the tables it uses, so plans of the same length (and the autotuner's candidates) build
+// each table once.  Returns the table's device pointer in *out; `build` fills a fresh buffer
+// on a miss (with the plan's device current).
+int cached_table(fyg_plan* pl, const std::string& key, const std::function<int(DevBuf&)>& build, const void** out);
 
 }  // namespace fyg
 
@@ -116,8 +117,7 @@ struct fyg_plan {
     int compute_bytes = 8;    // bytes of one compute complex
     std::vector<fyg::PassDesc> fwd, inv;
     // device tables
-    std::vector<std::unique_ptr<fyg::DevBuf>> tables;
-    std::map<std::string, const void*> tiled_tables;   // thread-order tables by key (owned by `tables`)
+    std::vector<std::shared_ptr<fyg::DevBuf>> tables;   // read-only, shared through the table cache
     fyg::DevBuf scratch0, scratch1, x0buf, dcbuf, errword;
     fyg::DevBuf stage_in, stage_out;   // staging for host pointers
     size_t stage_in_bytes = 0;

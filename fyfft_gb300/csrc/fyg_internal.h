@@ -49,7 +49,7 @@ using ConstUploader = cudaError_t (*)(const CodeletConsts<float>&, const Codelet
 bool register_const_uploader(ConstUploader f);
 
 // Device RNG fill (fyg_fill_random_device).
-cudaError_t launch_fill_random(uint64_t seed, int dist, int dtype, size_t n, void* out,
+cudaError_t launch_fill_random(uint64_t seed, int dist, int dtype, size_t first, size_t n, void* out,
                                cudaStream_t st);
 
 // Small helper kernels.

@@ -79,6 +79,52 @@ int DevBuf::upload(const void* host, size_t n) {
     return FYG_OK;
 }
 
+// ------------------------------------------------------------------------------------------
+// Table cache
+// ------------------------------------------------------------------------------------------
+
+namespace {
+struct TableCache {
+    std::mutex mu;
+    std::map<std::string, std::shared_ptr<DevBuf>> map;
+    uint64_t hits = 0, misses = 0;
+};
+// Heap-allocated and never destroyed: entries can outlive the CUDA runtime at process exit
+// (fyg_plan_cache_clear releases what no plan uses).
+TableCache& table_cache() {
+    static TableCache* c = new TableCache();
+    return *c;
+}
+}  // namespace
+
+int cached_table(fyg_plan* pl, const std::string& key, const std::function<int(DevBuf&)>& build, const void** out) {
+    const std::string k = "dev" + std::to_string(pl->device) + ":" + key;
+    TableCache& tc = table_cache();
+    {
+        std::lock_guard<std::mutex> lk(tc.mu);
+        auto it = tc.map.find(k);
+        if (it != tc.map.end()) {
+            ++tc.hits;
+            pl->tables.push_back(it->second);
+            *out = it->second->ptr;
+            return FYG_OK;
+        }
+        ++tc.misses;
+    }
+    // built without the lock: building a spectrum creates (and caches) a sub-plan
+    auto buf = std::make_shared<DevBuf>();
+    const int rc = build(*buf);
+    if (rc) return rc;
+    {
+        std::lock_guard<std::mutex> lk(tc.mu);
+        auto ins = tc.map.emplace(k, buf);
+        if (!ins.second) buf = ins.first->second;   // built concurrently by another thread
+    }
+    pl->tables.push_back(buf);
+    *out = buf->ptr;
+    return FYG_OK;
+}
+
 FastDiv make_fastdiv(uint32_t d) {
     FastDiv f;
     f.d = d;
@@ -269,6 +315,7 @@ static thread_local uint64_t t_conv_len = 0;
 static thread_local int t_order = 0;  // 1: reversed pass order
 static thread_local size_t t_idist = 0, t_odist = 0;  // user layout of the next plan (0: contiguous)
 static thread_local int t_cols = 0;   // single-pass: transforms per CTA (threads per transform = T/C)
+static thread_local int t_threads = 0;  // single-pass: thread policy of single_pass_threads
 
 bool split_passes(uint64_t L, int cb, bool conv, std::vector<int>& out) {
     std::vector<int> divs;
@@ -385,26 +432,29 @@ void host_two_level(uint64_t L, int cb, std::vector<unsigned char>& hi, std::vec
 }
 
 static int upload_local_table(fyg_plan* pl, int R, int cb, const void** dptr) {
-    auto buf = std::make_unique<DevBuf>();
-    const std::vector<unsigned char> h = host_local_table(R, cb);
-    const int rc = buf->upload(h.data(), h.size());
-    if (rc) return rc;
-    *dptr = buf->ptr;
-    pl->tables.push_back(std::move(buf));
-    return FYG_OK;
+    return cached_table(pl, "local:" + std::to_string(R) + ":" + std::to_string(cb), [&](DevBuf& b) {
+        const std::vector<unsigned char> h = host_local_table(R, cb);
+        return b.upload(h.data(), h.size());
+    }, dptr);
 }
 
+// one buffer: the hi table, then the lo table (both 16-byte entries)
 static int upload_two_level(fyg_plan* pl, uint64_t L, int cb, const void** hi, const void** lo, int* shift) {
     std::vector<unsigned char> th, tl;
-    host_two_level(L, cb, th, tl, shift);
-    auto bh = std::make_unique<DevBuf>(), bl = std::make_unique<DevBuf>();
-    int rc = bh->upload(th.data(), th.size());
-    if (!rc) rc = bl->upload(tl.data(), tl.size());
+    size_t hi_bytes = 0;
+    int s = 0;
+    host_two_level(L, cb, th, tl, &s);   // cheap next to the plan's other work: O(sqrt L) entries
+    hi_bytes = th.size();
+    const void* base = nullptr;
+    const int rc = cached_table(pl, "twolevel:" + std::to_string(L) + ":" + std::to_string(cb), [&](DevBuf& b) {
+        std::vector<unsigned char> all(th);
+        all.insert(all.end(), tl.begin(), tl.end());
+        return b.upload(all.data(), all.size());
+    }, &base);
     if (rc) return rc;
-    *hi = bh->ptr;
-    *lo = bl->ptr;
-    pl->tables.push_back(std::move(bh));
-    pl->tables.push_back(std::move(bl));
+    *hi = base;
+    *lo = static_cast<const unsigned char*>(base) + hi_bytes;
+    *shift = s;
     return FYG_OK;
 }
 
@@ -417,6 +467,7 @@ struct ConvTables {
     const int* gather = nullptr;
     const int* scatter = nullptr;
     const void* spectrum = nullptr;
+    std::string src_key;      // identifies the transform these tables belong to (cache keys)
 };
 
 struct PipeSpec {
@@ -424,6 +475,7 @@ struct PipeSpec {
     uint64_t L;               // algorithm length
     std::vector<int> prad;    // pass radices (size 1 for single-pass)
     int C;                    // columns per tile (single-pass: transforms per CTA)
+    int threads = 0;          // single-pass: thread policy (single_pass_threads)
 };
 
 int pick_variant(int compute_cb, int tin_cb, int tout_cb, int cls) {
@@ -440,6 +492,37 @@ int threads_for(int R, int C, int maxt) {
     t = (t + 31) / 32 * 32;
     t = std::max(t, 64);
     return std::min(t, maxt);
+}
+
+// Single-pass tiles (whole transforms per CTA).
+// Transforms per CTA: `requested` (the autotuner's choice) or about 4096 (FP32) / 2048 (FP64)
+// points per CTA; at most the batch and 256, and 1 when C transforms would not fit in shared
+// memory.
+int single_pass_cols(int cb, int L, size_t batch, int requested) {
+    int C = requested ? requested : std::max(1, (cb == 8 ? 4096 : 2048) / L);
+    C = (int)std::min<uint64_t>((uint64_t)C, batch);
+    C = std::max(std::min(C, 256), 1);
+    if (smem_for(cb, L, C, true) > kSmemLimit) C = 1;
+    return C;
+}
+
+// Threads per CTA of a single-pass tile: `requested` policy 0 = about 16 points per thread
+// (throughput: many CTAs per SM), 1 = one thread per butterfly of the stage with the most
+// butterflies (latency: the few CTAs of a small batch finish each stage in one step).
+int single_pass_threads(int L, int C, const std::vector<int>& rad, int requested) {
+    if (requested == 1 && !rad.empty()) {
+        const int rmin = *std::min_element(rad.begin(), rad.end());
+        int t = (L / rmin) * C;
+        t = (t + 31) / 32 * 32;
+        return std::max(64, std::min(t, kMaxThreads));
+    }
+    return threads_for(L, C, kMaxThreads);
+}
+
+// Whether a 13-smooth length runs as one tile pass (whole transform per CTA) within `cap`
+// bytes of shared memory.
+bool single_pass_fits(int cb, uint64_t n, size_t cap) {
+    return is_smooth(n, 13) && n <= 16384 && tile_fits(cb, (int)n, 1, true) && smem_for(cb, (int)n, 1, true) <= cap;
 }
 
 static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
@@ -521,7 +604,7 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
         }
         const int rmax = *std::max_element(rad.begin(), rad.end());
         const int cls = tile_class(cb, rmax);
-        d.threads = threads_for(R, C, kMaxThreads);
+        d.threads = single ? single_pass_threads(R, C, rad, ps.threads) : threads_for(R, C, kMaxThreads);
         d.kv = pick_variant(cb, (int)d.in_elem_bytes, (int)d.out_elem_bytes, cls);
         d.smem = smem_for(cb, R, C, single);
         // register-resident kernel for the tile lengths it is compiled for (FP32; not for the
@@ -539,23 +622,21 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
             d.threads = ft;
             d.smem = fsm;
             // thread-order tables (shared by the forward and inverse pipelines)
+            // keyed by content: the source table's own key (which transform's chirp or spectrum)
+            // and the tile geometry
             auto tiled = [&](const std::string& key, uint64_t total, int kind, const void* src, int64_t nvalid,
                              int conj, const void** outp) -> int {
-                auto it = pl->tiled_tables.find(key);
-                if (it != pl->tiled_tables.end()) { *outp = it->second; return FYG_OK; }
-                auto buf = std::make_unique<DevBuf>();
-                int rc = buf->alloc(total * sizeof(float2));
-                if (rc) return rc;
-                cudaError_t e = launch_fast_table(static_cast<float2*>(buf->ptr), total, R, kind, (uint64_t)p.Lr, L,
-                                                  (uint64_t)p.Rr, static_cast<const float2*>(src), nvalid, conj, 0);
-                if (e == cudaSuccess) e = cudaStreamSynchronize(0);
-                if (e != cudaSuccess) return cuda_error(e, "thread-order table");
-                *outp = buf->ptr;
-                pl->tiled_tables[key] = buf->ptr;
-                pl->tables.push_back(std::move(buf));
-                return FYG_OK;
+                return cached_table(pl, "tiled:" + key, [&](DevBuf& b) {
+                    int rc = b.alloc(total * sizeof(float2));
+                    if (rc) return rc;
+                    cudaError_t e = launch_fast_table(static_cast<float2*>(b.ptr), total, R, kind, (uint64_t)p.Lr, L,
+                                                      (uint64_t)p.Rr, static_cast<const float2*>(src), nvalid, conj, 0);
+                    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+                    return e == cudaSuccess ? FYG_OK : cuda_error(e, "thread-order table");
+                }, outp);
             };
-            const std::string sh = std::to_string(R) + ":" + std::to_string(Ns) + ":" + std::to_string(L);
+            const std::string sh = std::to_string(R) + ":" + std::to_string(Ns) + ":" + std::to_string(L) + ":" +
+                                   ct.src_key;
             int rc = FYG_OK;
             if (p.Ns > 1 && p.load_mode == LD_PLAIN) {
                 rc = tiled("tw:" + sh, Ns * (uint64_t)R, 0, nullptr, 0, 0, &p.tw_tiled);
@@ -578,16 +659,27 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
 // FP64 transform of a host vector on the GPU (used to precompute convolution spectra).
 static int gpu_fft_f64(size_t n, const std::vector<double2>& h, std::vector<double2>& H);
 
+// Spectrum of a convolution kernel: FP64 GPU FFT of the long-double kernel, rounded once to the
+// compute type.
+static int upload_spectrum(DevBuf& b, const std::vector<double2>& kernel_time, int cb) {
+    const size_t M = kernel_time.size();
+    std::vector<double2> H;
+    int rc = gpu_fft_f64(M, kernel_time, H);
+    if (rc) return rc;
+    if (cb == 8) {
+        std::vector<float2> Hf(M);
+        for (size_t i = 0; i < M; ++i) Hf[i] = make_float2((float)H[i].x, (float)H[i].y);
+        return b.upload(Hf.data(), M * sizeof(float2));
+    }
+    return b.upload(H.data(), M * sizeof(double2));
+}
+
 static int make_plan(fyg_plan* pl) {
     const uint64_t n = pl->n;
     const int io_cb = pl->dtype == FYG_C32 ? 8 : 16;
     PipeSpec ps;
     ps.C = 1;
     ConvTables ct;
-    std::vector<double2> kernel_time;   // convolution kernel (time domain), FP64
-    std::vector<int> gather, scatter;
-    std::vector<float2> chirp_f;
-    std::vector<double2> chirp_d;
 
     if (n == 1) {
         pl->strategy = GS_COPY;
@@ -599,8 +691,7 @@ static int make_plan(fyg_plan* pl) {
     const size_t single_cap = (pl->flags & FYG_FLAG_SMALL_TILES)
                                   ? (t_batch_single_cap ? std::min(t_batch_single_cap, kSmemLimit) : (100u << 10))
                                   : kSmemLimit;
-    if (is_smooth(n, 13) && n <= 16384 && tile_fits(io_cb, (int)n, 1, true) &&
-        smem_for(io_cb, (int)n, 1, true) <= single_cap) {
+    if (single_pass_fits(io_cb, n, single_cap)) {
         ps.kind = GS_SINGLE;
         ps.L = n;
         ps.prad = {(int)n};
@@ -656,13 +747,8 @@ static int make_plan(fyg_plan* pl) {
     }
     const int P = (int)ps.prad.size();
     if (P == 1) {
-        // several transforms per CTA for small lengths
-        const int target = cb == 8 ? 4096 : 2048;
-        int C = t_cols ? t_cols : std::max(1, target / (int)ps.L);
-        C = (int)std::min<uint64_t>((uint64_t)C, pl->batch);
-        C = std::min(C, 256);
-        ps.C = std::max(C, 1);
-        if (smem_for(cb, (int)ps.L, ps.C, true) > kSmemLimit) ps.C = 1;
+        ps.C = single_pass_cols(cb, (int)ps.L, pl->batch, t_cols);
+        ps.threads = t_threads;
     }
     // ---- chunking: keep the scratch of one chunk L2-resident ----
     const int K = conv ? 2 * P - 1 : P;
@@ -701,92 +787,90 @@ static int make_plan(fyg_plan* pl) {
         rc = upload_two_level(pl, ps.L, cb, &tw_hi, &tw_lo, &tw_shift);
         if (rc) return rc;
     }
+    const std::string cbs = std::to_string(cb);
     if (ps.kind == GS_BLUESTEIN) {
         // chirp w[k] = exp(+i pi (k^2 mod 2N) / N), exact integer reduction, long double
         const uint64_t twoN = 2 * n, M = ps.L;
-        std::vector<long double> wc(n), ws(n);
-        for (uint64_t k = 0; k < n; ++k) {
-            const uint64_t sq = mulmod(k, k, twoN);
-            const long double a = kTwoPiL * 0.5L * (long double)sq / (long double)n;
-            wc[k] = cosl(a);
-            ws[k] = sinl(a);
-        }
-        kernel_time.assign(M, make_double2(0, 0));
-        kernel_time[0] = make_double2((double)wc[0], (double)ws[0]);
-        for (uint64_t k = 1; k < n; ++k) {
-            kernel_time[k] = make_double2((double)wc[k], (double)ws[k]);
-            kernel_time[M - k] = kernel_time[k];
-        }
-        auto buf = std::make_unique<DevBuf>();
-        if (cb == 8) {
-            chirp_f.resize(n);
-            for (uint64_t k = 0; k < n; ++k) chirp_f[k] = make_float2((float)wc[k], (float)ws[k]);
-            rc = buf->upload(chirp_f.data(), n * sizeof(float2));
-        } else {
-            chirp_d.resize(n);
-            for (uint64_t k = 0; k < n; ++k) chirp_d[k] = make_double2((double)wc[k], (double)ws[k]);
-            rc = buf->upload(chirp_d.data(), n * sizeof(double2));
-        }
+        std::vector<long double> wc, ws;
+        auto chirp_ld = [&]() {
+            if (!wc.empty()) return;
+            wc.resize(n);
+            ws.resize(n);
+            for (uint64_t k = 0; k < n; ++k) {
+                const uint64_t sq = mulmod(k, k, twoN);
+                const long double a = kTwoPiL * 0.5L * (long double)sq / (long double)n;
+                wc[k] = cosl(a);
+                ws[k] = sinl(a);
+            }
+        };
+        ct.src_key = "B" + std::to_string(n) + ":" + std::to_string(M) + ":" + cbs;
+        rc = cached_table(pl, "chirp:" + std::to_string(n) + ":" + cbs, [&](DevBuf& b) {
+            chirp_ld();
+            if (cb == 8) {
+                std::vector<float2> c(n);
+                for (uint64_t k = 0; k < n; ++k) c[k] = make_float2((float)wc[k], (float)ws[k]);
+                return b.upload(c.data(), n * sizeof(float2));
+            }
+            std::vector<double2> c(n);
+            for (uint64_t k = 0; k < n; ++k) c[k] = make_double2((double)wc[k], (double)ws[k]);
+            return b.upload(c.data(), n * sizeof(double2));
+        }, &ct.chirp);
         if (rc) return rc;
-        ct.chirp = buf->ptr;
-        pl->tables.push_back(std::move(buf));
+        // the convolution kernel: the chirp and its mirror image, zero in between
+        rc = cached_table(pl, "spectrum:" + ct.src_key, [&](DevBuf& b) {
+            chirp_ld();
+            std::vector<double2> kt(M, make_double2(0, 0));
+            kt[0] = make_double2((double)wc[0], (double)ws[0]);
+            for (uint64_t k = 1; k < n; ++k) {
+                kt[k] = make_double2((double)wc[k], (double)ws[k]);
+                kt[M - k] = kt[k];
+            }
+            return upload_spectrum(b, kt, cb);
+        }, &ct.spectrum);
+        if (rc) return rc;
     } else if (ps.kind == GS_RADER) {
         const uint64_t Lc = n - 1, M = ps.L, g = primitive_root(n), ginv = powmod(g, n - 2, n);
-        gather.assign(M, -1);
-        scatter.assign(M, -1);
         std::vector<uint64_t> gp(Lc);
+        std::vector<int> gi(Lc);
         uint64_t cur = 1, curi = 1;
         for (uint64_t i = 0; i < Lc; ++i) {
             gp[i] = cur;
-            gather[i] = (int)curi;
+            gi[i] = (int)curi;
             cur = mulmod(cur, g, n);
             curi = mulmod(curi, ginv, n);
         }
-        kernel_time.assign(M, make_double2(0, 0));
-        if (M == Lc) {
-            for (uint64_t q = 0; q < Lc; ++q) scatter[q] = (int)gp[q];
-            for (uint64_t p = 0; p < Lc; ++p) {
-                long double c, s;
-                twiddle_ld(gp[p], n, &c, &s);
-                kernel_time[p] = make_double2((double)c, (double)s);
+        ct.src_key = "R" + std::to_string(n) + ":" + std::to_string(M) + ":" + cbs;
+        // gather (M ints) then scatter (M ints)
+        const void* maps = nullptr;
+        rc = cached_table(pl, "rader:" + std::to_string(n) + ":" + std::to_string(M), [&](DevBuf& b) {
+            std::vector<int> gs(2 * M, -1);
+            for (uint64_t i = 0; i < Lc; ++i) gs[i] = gi[i];
+            int* scatter = gs.data() + M;
+            if (M == Lc) {
+                for (uint64_t q = 0; q < Lc; ++q) scatter[q] = (int)gp[q];
+            } else {
+                // zero-padded linear convolution; outputs q in [L-1, 2L-1) carry the cyclic result
+                for (uint64_t q = Lc - 1; q < 2 * Lc - 1; ++q) scatter[q] = (int)gp[q % Lc];
             }
-        } else {
-            // zero-padded linear convolution; outputs q in [L-1, 2L-1) carry the cyclic result
-            for (uint64_t q = Lc - 1; q < 2 * Lc - 1; ++q) scatter[q] = (int)gp[q % Lc];
-            for (uint64_t m = 0; m < M; ++m) {
-                long double c, s;
-                twiddle_ld(gp[m % Lc], n, &c, &s);
-                kernel_time[m] = make_double2((double)c, (double)s);
-            }
-        }
-        auto bg = std::make_unique<DevBuf>(), bs = std::make_unique<DevBuf>();
-        rc = bg->upload(gather.data(), M * sizeof(int));
-        if (!rc) rc = bs->upload(scatter.data(), M * sizeof(int));
+            return b.upload(gs.data(), 2 * M * sizeof(int));
+        }, &maps);
         if (rc) return rc;
-        ct.gather = reinterpret_cast<const int*>(bg->ptr);
-        ct.scatter = reinterpret_cast<const int*>(bs->ptr);
-        pl->tables.push_back(std::move(bg));
-        pl->tables.push_back(std::move(bs));
+        ct.gather = static_cast<const int*>(maps);
+        ct.scatter = static_cast<const int*>(maps) + M;
+        // the convolution kernel w^(g^p), periodically extended for the zero-padded form
+        rc = cached_table(pl, "spectrum:" + ct.src_key, [&](DevBuf& b) {
+            std::vector<double2> kt(M, make_double2(0, 0));
+            for (uint64_t m = 0; m < M; ++m) {
+                long double c, sn;
+                twiddle_ld(gp[m % Lc], n, &c, &sn);
+                kt[m] = make_double2((double)c, (double)sn);
+            }
+            return upload_spectrum(b, kt, cb);
+        }, &ct.spectrum);
+        if (rc) return rc;
         rc = pl->x0buf.alloc(pl->chunk * cb);
         if (!rc) rc = pl->dcbuf.alloc(pl->chunk * cb);
         if (rc) return rc;
-    }
-    if (conv) {
-        // spectrum of the convolution kernel: FP64 GPU FFT of the long-double kernel, rounded once
-        std::vector<double2> H;
-        rc = gpu_fft_f64(ps.L, kernel_time, H);
-        if (rc) return rc;
-        auto buf = std::make_unique<DevBuf>();
-        if (cb == 8) {
-            std::vector<float2> Hf(ps.L);
-            for (uint64_t i = 0; i < ps.L; ++i) Hf[i] = make_float2((float)H[i].x, (float)H[i].y);
-            rc = buf->upload(Hf.data(), ps.L * sizeof(float2));
-        } else {
-            rc = buf->upload(H.data(), ps.L * sizeof(double2));
-        }
-        if (rc) return rc;
-        ct.spectrum = buf->ptr;
-        pl->tables.push_back(std::move(buf));
     }
     // ---- scratch ----
     if (K >= 2) {
@@ -855,13 +939,17 @@ static int run_pipeline(fyg_plan* pl, const std::vector<PassDesc>& pipe, const v
     return FYG_OK;
 }
 
-static bool is_device_ptr(const void* ptr) {
+// 1: device memory of device `dev` or managed memory; 0: host memory; -1: device memory of
+// another device (its kernels would fault without peer access: rejected)
+static int device_ptr_kind(const void* ptr, int dev) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
         cudaGetLastError();
-        return false;
+        return 0;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return 1;
+    if (a.type == cudaMemoryTypeDevice) return a.device == dev ? 1 : -1;
+    return 0;
 }
 
 // Host input and output: the batch is cut into chunks; chunk i's host->device copy (copy-in
@@ -965,7 +1053,10 @@ static int execute_dir(fyg_plan* pl, const void* in, void* out, bool inverse, do
         }
     } scope(pl->device);
     const size_t bytes = pl->n * pl->batch * io_cb;
-    const bool din = is_device_ptr(in), dout = is_device_ptr(out);
+    const int kin = device_ptr_kind(in, pl->device), kout = device_ptr_kind(out, pl->device);
+    if (kin < 0 || kout < 0)
+        return set_error(FYG_ERR_INVALID_ARG, "buffers on another device than the plan's");
+    const bool din = kin > 0, dout = kout > 0;
     if (!din && !dout && pl->strategy != GS_COPY && pl->batch >= 2 && bytes >= (8u << 20))
         return execute_host_overlapped(pl, in, out, inverse, scale_mul, st);
     const void* din_p = in;
@@ -1006,9 +1097,9 @@ static int gpu_fft_f64(size_t n, const std::vector<double2>& h, std::vector<doub
     const size_t keep_idist = t_idist, keep_odist = t_odist;
     t_order = 0;
     t_idist = t_odist = 0;
-    const int keep_cap = t_radix_cap, keep_cols = t_cols;
+    const int keep_cap = t_radix_cap, keep_cols = t_cols, keep_threads = t_threads;
     t_max_pass_r = t_conv_len = 0;
-    t_radix_cap = t_cols = 0;
+    t_radix_cap = t_cols = t_threads = 0;
     int rc = fyg_plan_create(n, FYG_C64, 1, 0, &sub);
     t_max_pass_r = keep_r;
     t_conv_len = keep_m;
@@ -1017,6 +1108,7 @@ static int gpu_fft_f64(size_t n, const std::vector<double2>& h, std::vector<doub
     t_odist = keep_odist;
     t_radix_cap = keep_cap;
     t_cols = keep_cols;
+    t_threads = keep_threads;
     if (rc) return rc;
     DevBuf a, b;
     rc = a.upload(h.data(), n * sizeof(double2));
@@ -1059,16 +1151,18 @@ void set_batch_tile_options(int radix_cap, size_t single_cap_bytes) {
 
 // plan creation with explicit schedule options (0 = default); used by the autotuner
 int plan_create_opts(size_t n, int dtype, size_t batch, int flags, uint64_t max_pass_radix, uint64_t conv_length,
-                     int cols, int order, fyg_plan** out) {
+                     int cols, int order, int threads, fyg_plan** out) {
     t_max_pass_r = max_pass_radix;
     t_conv_len = conv_length;
     t_cols = cols;
     t_order = order;
+    t_threads = threads;
     const int rc = fyg_plan_create(n, dtype, batch, flags & ~FYG_FLAG_AUTOTUNED, out);
     t_max_pass_r = 0;
     t_conv_len = 0;
     t_cols = 0;
     t_order = 0;
+    t_threads = 0;
     return rc;
 }
 }  // namespace fyg
@@ -1089,7 +1183,7 @@ int fyg_plan_create_layout(size_t n, int dtype, size_t batch, size_t idist, size
 
 int fyg_plan_create_ex(size_t n, int dtype, size_t batch, int flags, size_t max_pass_radix, size_t conv_length,
                        fyg_plan** out) {
-    return plan_create_opts(n, dtype, batch, flags & ~FYG_FLAG_AUTOTUNED, max_pass_radix, conv_length, 0, 0, out);
+    return plan_create_opts(n, dtype, batch, flags & ~FYG_FLAG_AUTOTUNED, max_pass_radix, conv_length, 0, 0, 0, out);
 }
 
 
@@ -1098,7 +1192,8 @@ int fyg_plan_create(size_t n, int dtype, size_t batch, int flags, fyg_plan** out
     if (flags & FYG_FLAG_AUTOTUNED) {
         TuneChoice tc;
         if (tune_lookup(n, dtype, &tc))
-            return plan_create_opts(n, dtype, batch, flags, tc.max_pass_radix, tc.conv_length, tc.cols, tc.order, out);
+            return plan_create_opts(n, dtype, batch, flags, tc.max_pass_radix, tc.conv_length, tc.cols, tc.order,
+                                    tc.threads, out);
         flags &= ~FYG_FLAG_AUTOTUNED;
     }
     if (!out) return set_error(FYG_ERR_NULL_PTR, "out is null");
@@ -1223,6 +1318,28 @@ int fyg_execute_adjoint(fyg_plan* plan, const void* g, void* out, double scale, 
     return execute_dir(plan, g, out, true, scale * (double)plan->n, (cudaStream_t)stream);
 }
 
+int fyg_plan_cache_stats(size_t* entries, size_t* bytes, uint64_t* hits, uint64_t* misses) {
+    TableCache& tc = table_cache();
+    std::lock_guard<std::mutex> lk(tc.mu);
+    size_t b = 0;
+    for (auto& kv : tc.map) b += kv.second->bytes;
+    if (entries) *entries = tc.map.size();
+    if (bytes) *bytes = b;
+    if (hits) *hits = tc.hits;
+    if (misses) *misses = tc.misses;
+    return FYG_OK;
+}
+
+int fyg_plan_cache_clear(void) {
+    TableCache& tc = table_cache();
+    std::lock_guard<std::mutex> lk(tc.mu);
+    for (auto it = tc.map.begin(); it != tc.map.end();) {
+        if (it->second.use_count() == 1) it = tc.map.erase(it);   // no live plan holds it
+        else ++it;
+    }
+    return FYG_OK;
+}
+
 int fyg_strategy(size_t n) { return ref_strategy(n); }
 
 int fyg_gpu_strategy(size_t n) {
@@ -1244,16 +1361,25 @@ int fyg_plan_info(const fyg_plan* plan, size_t* conv_length, int* passes, int* s
 const char* fyg_last_error_string(void) { return last_error(); }
 
 int fyg_fill_random(uint64_t seed, int dist, int dtype, size_t n_complex, void* out) {
+    return fyg_fill_random_at(seed, dist, dtype, 0, n_complex, out);
+}
+
+int fyg_fill_random_at(uint64_t seed, int dist, int dtype, size_t first, size_t n_complex, void* out) {
     if (!out && n_complex) return set_error(FYG_ERR_NULL_PTR, "null buffer");
     if (dtype != FYG_C32 && dtype != FYG_C64) return set_error(FYG_ERR_INVALID_ARG, "bad dtype");
-    fill_random_host(seed, dist, dtype, n_complex, out);
+    fill_random_host(seed, dist, dtype, first, n_complex, out);
     return FYG_OK;
 }
 
 int fyg_fill_random_device(uint64_t seed, int dist, int dtype, size_t n_complex, void* out, void* stream) {
+    return fyg_fill_random_device_at(seed, dist, dtype, 0, n_complex, out, stream);
+}
+
+int fyg_fill_random_device_at(uint64_t seed, int dist, int dtype, size_t first, size_t n_complex, void* out,
+                              void* stream) {
     if (!out && n_complex) return set_error(FYG_ERR_NULL_PTR, "null buffer");
     if (dtype != FYG_C32 && dtype != FYG_C64) return set_error(FYG_ERR_INVALID_ARG, "bad dtype");
-    cudaError_t e = launch_fill_random(seed, dist, dtype, n_complex, out, (cudaStream_t)stream);
+    cudaError_t e = launch_fill_random(seed, dist, dtype, first, n_complex, out, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_error(e, "fill_random_device");
     return FYG_OK;
 }

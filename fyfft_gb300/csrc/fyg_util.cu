@@ -94,27 +94,28 @@ __host__ __device__ inline void rand_pair(uint64_t seed, uint64_t i, int dist, d
     }
 }
 
-__global__ void k_fill_random(uint64_t seed, int dist, int dtype, size_t n, void* out) {
+__global__ void k_fill_random(uint64_t seed, int dist, int dtype, size_t first, size_t n, void* out) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         double re, im;
-        rand_pair(seed, i, dist, &re, &im);
+        rand_pair(seed, first + i, dist, &re, &im);
         if (dtype == 0) reinterpret_cast<float2*>(out)[i] = make_float2((float)re, (float)im);
         else reinterpret_cast<double2*>(out)[i] = make_double2(re, im);
     }
 }
 
-cudaError_t launch_fill_random(uint64_t seed, int dist, int dtype, size_t n, void* out, cudaStream_t st) {
+cudaError_t launch_fill_random(uint64_t seed, int dist, int dtype, size_t first, size_t n, void* out,
+                               cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
-    k_fill_random<<<blocks, 256, 0, st>>>(seed, dist, dtype, n, out);
+    k_fill_random<<<blocks, 256, 0, st>>>(seed, dist, dtype, first, n, out);
     return cudaGetLastError();
 }
 
-void fill_random_host(uint64_t seed, int dist, int dtype, size_t n, void* out) {
+void fill_random_host(uint64_t seed, int dist, int dtype, size_t first, size_t n, void* out) {
     auto work = [=](size_t lo, size_t hi) {
         for (size_t i = lo; i < hi; ++i) {
             double re, im;
-            rand_pair(seed, i, dist, &re, &im);
+            rand_pair(seed, first + i, dist, &re, &im);
             if (dtype == 0) {
                 reinterpret_cast<float*>(out)[2 * i] = (float)re;
                 reinterpret_cast<float*>(out)[2 * i + 1] = (float)im;

@@ -61,6 +61,7 @@ extern "C" {
 
 typedef struct fyg_plan fyg_plan;
 typedef struct fyg_batch fyg_batch;
+typedef struct fyg_multi fyg_multi;
 
 /* Creates a plan for `batch` contiguous transforms of length n (n >= 1).
  * Replaces fy::fft::FFT1D_C2C_invoker::FFT1D_C2C_invoker(std::size_t) (foye_FFT.hpp:101-126):
@@ -85,6 +86,16 @@ int fyg_autotune(size_t n, int dtype, size_t batch, const char* cache_path, doub
 
 /* Releases the plan and its device tables and scratch. */
 int fyg_plan_destroy(fyg_plan* plan);
+
+/* Process-wide table cache.  Plans share their read-only device tables (twiddles, chirps,
+ * Rader index maps, convolution spectra, thread-order tables) through a cache keyed by device
+ * and content, so creating a second plan of a length (or the autotuner's candidates) reuses
+ * them; each plan keeps only its scratch.  Replaces the reference's process-wide registry of
+ * length -> engine with static tables (src/foye_FFT_radix_wrap.hpp:81-85).
+ * fyg_plan_cache_stats: entries, device bytes held, lookups that hit and missed.
+ * fyg_plan_cache_clear: frees the tables no live plan uses (safe at any time). */
+int fyg_plan_cache_stats(size_t* entries, size_t* bytes, uint64_t* hits, uint64_t* misses);
+int fyg_plan_cache_clear(void);
 
 /* Runs the batch: direction FYG_FORWARD or FYG_INVERSE (1/N).  `in` and `out` are device
  * pointers, or host pointers (staged through device buffers and synchronized before return).
@@ -168,16 +179,38 @@ int fyg_batch_inject_stall(fyg_batch* batch, int enable, int timeout_ms);
 int fyg_batch_execute_plain(fyg_batch* batch, const void* in, void* out, int direction,
                             void* stream);
 
+/* Batch sharding across devices (no collective: transforms are independent; the reference runs
+ * one transform per dispatch<>() call, foye_FFT.hpp:128-151, and its plans are one per thread).
+ * fyg_partition: contiguous shards of near-equal cost -- bounds[0..parts] with bounds[0] = 0 and
+ * bounds[parts] = count; lengths == NULL for a uniform batch (equal counts), else cost
+ * n log2 n per transform.  The same split serves one process per device (each rank runs
+ * [bounds[rank], bounds[rank+1])) and fyg_multi_create, one plan and stream per device.
+ * fyg_multi_execute: host buffers of the whole batch, every shard staged to its device by its
+ * own host thread; returns when all outputs are in host memory.
+ * fyg_multi_execute_device: ins[i] / outs[i] hold shard i on devices[i]; asynchronous,
+ * fyg_multi_synchronize waits.  A device may appear more than once. */
+int fyg_partition(const size_t* lengths, size_t count, int parts, size_t* bounds);
+int fyg_multi_create(size_t n, int dtype, size_t batch, int flags, const int* devices, int ndev, fyg_multi** out);
+int fyg_multi_shards(const fyg_multi* multi, int* ndev, size_t* bounds);
+int fyg_multi_execute(fyg_multi* multi, const void* in, void* out, int direction);
+int fyg_multi_execute_device(fyg_multi* multi, const void* const* ins, void* const* outs, int direction);
+int fyg_multi_synchronize(fyg_multi* multi);
+int fyg_multi_destroy(fyg_multi* multi);
+
 /* Allocation-free transform: no counterpart in the reference.  For callers that cannot call
- * cudaMalloc (code running during CUDA graph capture, host applications that own all device
- * memory and pass a plugin only its buffers, latency-bound loops that cannot take the
- * synchronization an allocation may cause).  Runs `batch` contiguous transforms of a 13-smooth
- * length n with the multi-pass kernel; its scratch and twiddle tables live in a fixed 20 MiB
- * file-scope device array (held by every GPU that loads the library until exit).  Limit:
- * n * batch * element size <= 16 MiB (half that when n needs three or more passes); larger
- * sizes return FYG_ERR_INVALID_LENGTH.  in/out must be device pointers; nothing is allocated.
- * The first call on a device resolves the array's address and uploads constants, so make it
- * before any stream capture.  All calls share the array: calls that overlap on the GPU race. */
+ * cudaMalloc: a host application that owns all device memory and gives a plugin only its input
+ * and output buffers (an allocation inside the plugin could fail or break its memory budget),
+ * and a loop with a latency budget that cannot take the device-wide synchronization cudaMalloc
+ * or cudaFree may cause.  Runs `batch` contiguous transforms of a 13-smooth length n with the
+ * multi-pass kernel; its scratch and twiddle tables live in a fixed 20 MiB file-scope device
+ * array (held by every GPU that loads the library until exit).  Limit: n * batch * element
+ * size <= 16 MiB (half that when n needs three or more passes); larger sizes return
+ * FYG_ERR_INVALID_LENGTH.  in/out must be device pointers of the current device; nothing is
+ * allocated and nothing is copied from the host: the twiddle tables are computed on the device
+ * into the array when n or the type differs from the previous call's.  The first call on a
+ * device does a one-time set-up (the array's address via cudaGetSymbolAddress and the codelet
+ * constants, both synchronous), so make it before any stream capture.  All calls share the
+ * array, which keeps the last call's contents: calls that overlap on the GPU race. */
 int fyg_execute_noalloc(size_t n, size_t batch, int dtype, int direction, const void* in, void* out,
                         void* stream);
 
@@ -192,6 +225,12 @@ int fyg_fill_random(uint64_t seed, int dist, int dtype, size_t n_complex, void* 
 /* Same stream generated on the device into device memory. */
 int fyg_fill_random_device(uint64_t seed, int dist, int dtype, size_t n_complex, void* out,
                            void* stream);
+
+/* Elements [first, first + n_complex) of the same stream (a shard of a larger batch), on the
+ * host or on the device. */
+int fyg_fill_random_at(uint64_t seed, int dist, int dtype, size_t first, size_t n_complex, void* out);
+int fyg_fill_random_device_at(uint64_t seed, int dist, int dtype, size_t first, size_t n_complex, void* out,
+                              void* stream);
 
 /* Library version string. */
 const char* fyg_version(void);

@@ -41,7 +41,8 @@ def test_cache_file_lists_every_length(cache):
     assert doc["device"] and torch.cuda.get_device_name(0) in doc["device"]
     for n in LENGTHS:
         e = doc["entries"][f"c32:{n}"]
-        assert e["ms"] > 0 and set(e) == {"max_pass_radix", "conv_length", "cols", "order", "ms"}
+        assert e["ms"] > 0 and set(e) == {"max_pass_radix", "conv_length", "cols", "order", "threads", "ms"}
+        assert e["threads"] in (0, 1)
 
 
 @pytest.mark.parametrize("n", LENGTHS)
@@ -82,7 +83,8 @@ def test_cache_for_another_device_is_ignored(tmp_path):
     path = str(tmp_path / "other.json")
     with open(path, "w") as f:
         f.write('{\n  "device": "some other GPU|1|1.0|1",\n  "entries": {\n'
-                '    "c32:1009": {"max_pass_radix": 0, "conv_length": 5000, "cols": 0, "order": 0, "ms": 1.0}\n  }\n}\n')
+                '    "c32:1009": {"max_pass_radix": 0, "conv_length": 5000, "cols": 0, "order": 0, "threads": 0, '
+                '"ms": 1.0}\n  }\n}\n')
     # tuning another length into that file replaces the foreign entries
     fg.autotune(2520, "complex64", 4, cache_path=path)
     doc = json.load(open(path))

@@ -1,9 +1,14 @@
-"""The allocation-free entry point (fyg_execute_noalloc) against the plan-based one.
+"""The allocation-free entry point (fyg_execute_noalloc) against the plan-based entry point and
+the FP64 oracle.
 
-Callers that cannot call cudaMalloc (graph capture, host applications that own all device
-memory, latency-bound loops) use fyg_execute_noalloc, whose scratch lives in a fixed device
-array inside the library.  This file runs last so a failure here leaves every other test run;
-it passes alone in a fresh process and after the rest of the suite."""
+Who calls it: a host application that owns all device memory (it sizes one pool up front and
+gives each plugin only its input and output buffers) cannot let this library allocate behind
+its back, and a loop with a latency budget cannot take the device-wide synchronization that
+cudaMalloc / cudaFree may cause.  fyg_execute_noalloc keeps its scratch and twiddle tables in a
+fixed device array inside the library instead.  Each case makes two calls in a row on the same
+array (forward, then inverse on other data), so a stale table or intermediate from the first
+call would show in the second.  This file is collected last, so a failure here leaves every
+other test run; it passes alone in a fresh process and after the rest of the suite."""
 import ctypes
 
 import numpy as np
@@ -12,6 +17,7 @@ import pytest
 torch = pytest.importorskip("torch")
 
 import fyfft_gb300 as fg  # noqa: E402
+from oracle import oracle as O  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
@@ -52,8 +58,14 @@ def test_noalloc_matches_plan_path_twice_in_a_row(n, batch, dtype):
         ref = torch.empty(n * batch, dtype=tdt, device="cuda")
         plan.dispatch(inverse, x, ref)
         torch.cuda.synchronize()
-        err = rel_l2(y.cpu().numpy(), ref.cpu().numpy())
+        yh = y.cpu().numpy()
+        err = rel_l2(yh, ref.cpu().numpy())
         assert err <= tol, (n, batch, call, err, tol)
+        # first and last transform against the FP64 oracle
+        xh = x.cpu().numpy().reshape(batch, n)
+        for b in (0, batch - 1):
+            err_o = rel_l2(yh.reshape(batch, n)[b], O.fft(xh[b], inverse=inverse))
+            assert err_o <= tol, (n, batch, call, b, err_o, tol)
 
 
 def test_noalloc_rejects_sizes_beyond_its_array():
