@@ -30,6 +30,7 @@ FYG_C32, FYG_C64 = 0, 1
 FYG_FORWARD, FYG_INVERSE = 1, -1
 FYG_FLAG_CONV_FP64, FYG_FLAG_CONV_FP32, FYG_FLAG_NO_L2_CHUNK = 1, 2, 4
 FYG_FLAG_SMALL_TILES, FYG_FLAG_AUTOTUNED, FYG_FLAG_GENERIC_KERNELS = 8, 16, 32
+FYG_FLAG_WIDE_TILES = 64
 
 # every symbol include/fygpu.h declares
 EXPORTED_SYMBOLS = (

@@ -4,10 +4,11 @@
 //   single-pass lengths   transforms per CTA (C) and the thread policy (about 16 points per
 //                         thread, or one thread per butterfly of the widest stage), i.e. the
 //                         threads per transform
-//   multi-pass lengths    a cap on the pass radix (more, smaller passes or fewer, larger ones)
+//   multi-pass lengths    a cap on the pass radix (more, smaller passes or fewer, larger ones),
+//                         the pass order and the register-resident tile width (wide tiles)
 //   Rader / Bluestein     the convolution length (7-smooth lengths up to 8% above the minimum,
-//                         and for Bluestein the power of two), a cap on its pass radix and the
-//                         pass order (which radix the fused mid pass takes)
+//                         and for Bluestein the power of two), a cap on its pass radix, the
+//                         pass order (which radix the fused mid pass takes) and the tile width
 // FYG_AUTOTUNE_VERBOSE=1 lists every candidate's time on stderr.
 // Every candidate plan runs a forward batch on the current device (CUDA events, best of three
 // after a warm-up); the fastest is written to the cache under "c32:<n>" / "c64:<n>" together
@@ -75,19 +76,20 @@ void load(const std::string& path) {
         }
         char key[64];
         unsigned long long r = 0, m = 0;
-        int c = 0, o = 0, th = 0;
+        int c = 0, o = 0, th = 0, w = 0;
         double ms = 0;
-        const int got = std::sscanf(
-            line.c_str(),
-            " \"%63[^\"]\": {\"max_pass_radix\": %llu, \"conv_length\": %llu, \"cols\": %d, \"order\": %d, \"threads\": %d, \"ms\": %lf",
-            key, &r, &m, &c, &o, &th, &ms);
-        if (got == 7) {
+        const int got = std::sscanf(line.c_str(),
+                                    " \"%63[^\"]\": {\"max_pass_radix\": %llu, \"conv_length\": %llu, \"cols\": %d, "
+                                    "\"order\": %d, \"threads\": %d, \"wide\": %d, \"ms\": %lf",
+                                    key, &r, &m, &c, &o, &th, &w, &ms);
+        if (got == 8) {
             TuneChoice t;
             t.max_pass_radix = r;
             t.conv_length = m;
             t.cols = c;
             t.order = o;
             t.threads = th;
+            t.wide = w;
             t.ms = ms;
             g_cache.entries[key] = t;
         }
@@ -106,10 +108,10 @@ int save() {
         char buf[320];
         std::snprintf(buf, sizeof(buf),
                       "    \"%s\": {\"max_pass_radix\": %llu, \"conv_length\": %llu, \"cols\": %d, \"order\": %d, "
-                      "\"threads\": %d, \"ms\": %.6f}%s\n",
+                      "\"threads\": %d, \"wide\": %d, \"ms\": %.6f}%s\n",
                       kv.first.c_str(), (unsigned long long)kv.second.max_pass_radix,
                       (unsigned long long)kv.second.conv_length, kv.second.cols, kv.second.order, kv.second.threads,
-                      kv.second.ms, ++i < g_cache.entries.size() ? "," : "");
+                      kv.second.wide, kv.second.ms, ++i < g_cache.entries.size() ? "," : "");
         f << buf;
     }
     f << "  }\n}\n";
@@ -140,15 +142,17 @@ std::vector<TuneChoice> candidates(size_t n, int dtype, size_t batch) {
     const int cb = dtype == FYG_C32 ? 8 : 16;
     std::vector<TuneChoice> out;
     out.push_back(TuneChoice());
-    auto add = [&](uint64_t r, uint64_t m, int c, int o = 0, int th = 0) {
+    auto add = [&](uint64_t r, uint64_t m, int c, int o = 0, int th = 0, int w = 0) {
         TuneChoice t;
         t.max_pass_radix = r;
         t.conv_length = m;
         t.cols = c;
         t.order = o;
         t.threads = th;
+        t.wide = w;
         out.push_back(t);
     };
+    const int nwide = dtype == FYG_C32 ? 2 : 1;   // wide register-resident tiles: FP32 only
     // single-pass lengths: transforms per CTA x thread policy (threads per transform)
     auto add_single = [&](uint64_t m, uint64_t L) {
         for (int c : {1, 2, 4, 8, 16, 32, 64})
@@ -159,8 +163,11 @@ std::vector<TuneChoice> candidates(size_t n, int dtype, size_t batch) {
         if (single_pass_fits(cb, n, (size_t)-1)) {
             add_single(0, n);
         } else {
-            for (uint64_t r : {2048ull, 1024ull, 512ull, 256ull, 128ull}) add(r, 0, 0);
-            add(0, 0, 0, 1);
+            for (int w = 0; w < nwide; ++w) {
+                if (w) add(0, 0, 0, 0, 0, 1);
+                for (uint64_t r : {2048ull, 1024ull, 512ull, 256ull, 128ull}) add(r, 0, 0, 0, 0, w);
+                add(0, 0, 0, 1, 0, w);
+            }
         }
         return out;
     }
@@ -178,8 +185,10 @@ std::vector<TuneChoice> candidates(size_t n, int dtype, size_t batch) {
             add_single(m, m);
             continue;
         }
-        for (uint64_t r : {0ull, 256ull})
-            for (int o : {0, 1}) add(r, m, 0, o);
+        for (int o : {0, 1}) {
+            for (int w = 0; w < nwide; ++w) add(0, m, 0, o, 0, w);
+            add(256, m, 0, o);
+        }
     }
     return out;
 }
@@ -235,8 +244,8 @@ extern "C" int fyg_autotune(size_t n, int dtype, size_t batch, const char* cache
     const bool verbose = std::getenv("FYG_AUTOTUNE_VERBOSE") != nullptr;
     for (const TuneChoice& c : candidates(n, dtype, batch)) {
         fyg_plan* pl = nullptr;
-        if (plan_create_opts(n, dtype, batch, 0, c.max_pass_radix, c.conv_length, c.cols, c.order, c.threads, &pl) !=
-            FYG_OK)
+        if (plan_create_opts(n, dtype, batch, c.wide ? FYG_FLAG_WIDE_TILES : 0, c.max_pass_radix, c.conv_length, c.cols,
+                             c.order, c.threads, &pl) != FYG_OK)
             continue;
         double t = 1e30;
         bool ok = fyg_execute(pl, in.ptr, out.ptr, FYG_FORWARD, nullptr) == FYG_OK;
@@ -252,9 +261,10 @@ extern "C" int fyg_autotune(size_t n, int dtype, size_t batch, const char* cache
         fyg_plan_destroy(pl);
         if (verbose)
             std::fprintf(stderr,
-                         "fyg_autotune n=%zu max_pass_radix=%llu conv_length=%llu cols=%d order=%d threads=%d: %s %.4f ms\n",
+                         "fyg_autotune n=%zu max_pass_radix=%llu conv_length=%llu cols=%d order=%d threads=%d wide=%d: "
+                         "%s %.4f ms\n",
                          n, (unsigned long long)c.max_pass_radix, (unsigned long long)c.conv_length, c.cols, c.order,
-                         c.threads, ok ? "ok" : "failed", ok ? t : 0.0);
+                         c.threads, c.wide, ok ? "ok" : "failed", ok ? t : 0.0);
         if (ok && (!have || t < best.ms)) {
             best = c;
             best.ms = t;

@@ -55,11 +55,21 @@ template <int R_, int P_, int C_, int TWB_ = 4> struct FastShape {
         for (int t = 0; t < s; ++t) v *= radix(t);
         return v;
     }
+    // offset of stage s's block in the stage-twiddle table (blocks of radix(s) * ns(s) entries
+    // for s = 1 .. nst-1)
+    __host__ __device__ static constexpr int stage_off(int s) {
+        int o = 0;
+        for (int t = 1; t < s; ++t) o += radix(t) * ns(t);
+        return o;
+    }
     static constexpr size_t smem_bytes() { return (size_t)C * Rp * sizeof(float2); }
 };
 
 // The shapes in use: 256 threads per CTA (two CTAs per SM) up to R = 2048; 243 = 27 * 9 and
 // 343 = 7 * 7 * 7 for powers of three and seven (C divides their column counts 3^k / 7^k).
+// Wide shapes: 512 threads per CTA (one CTA per SM, the same 16 warps) with twice the columns,
+// so that every row segment a tile reads or writes is 64-256 contiguous bytes instead of 32-128
+// (FYG_FLAG_WIDE_TILES; the autotuner measures both).
 using FastR256 = FastShape<256, 16, 16>;
 using FastR512 = FastShape<512, 32, 16>;
 using FastR1024 = FastShape<1024, 32, 8>;
@@ -67,8 +77,25 @@ using FastR2048 = FastShape<2048, 32, 4>;
 using FastR4096 = FastShape<4096, 32, 4>;
 using FastR243 = FastShape<243, 27, 27, 3>;
 using FastR343 = FastShape<343, 7, 7, 7>;
+using FastR256W = FastShape<256, 16, 32>;
+using FastR512W = FastShape<512, 32, 32>;
+using FastR1024W = FastShape<1024, 32, 16>;
+using FastR2048W = FastShape<2048, 32, 8>;
 
 template <class S> __device__ __forceinline__ int fast_addr(int c, int n) { return c * S::Rp + n + S::pad(n); }
+
+// A thread's own points n = g + G i sit at own_base + own_off(i): the padding (g + G i) >> 5
+// splits into a per-thread part and a compile-time part when G is a multiple or a divisor of 32
+// (then g < G never carries into the padding); other shapes use fast_addr.
+template <class S> struct Own {
+    static constexpr bool linear = (S::G % 32 == 0) || (32 % S::G == 0);
+    __device__ static __forceinline__ int base(int c, int g) {
+        return c * S::Rp + g + ((S::G % 32 == 0) ? (g >> 5) : 0);
+    }
+    __host__ __device__ static constexpr int off(int i) {
+        return S::G * i + ((S::G % 32 == 0) ? i * (S::G / 32) : ((S::G * i) >> 5));
+    }
+};
 
 // One in-CTA Stockham stage over the thread's registers.  Non-final stages write their outputs
 // to shared memory and read the next stage's operands back (two barriers: the buffer is shared
@@ -77,7 +104,10 @@ template <class S, int ST>
 __device__ __forceinline__ void fast_stage(float2 (&v)[S::P], float2* sm, int c, int g, const float2* twl) {
     constexpr int r = S::radix(ST), ns = S::ns(ST), nb = S::P / r;
     constexpr bool last = ST == S::nst() - 1;
-    constexpr int twm = S::R / (ns * r);
+    // outputs base + m ns: linear in m (one per-thread address, compile-time offsets) when ns is
+    // a multiple of 32, or ns == 1 with r dividing 32 (base = j r stays inside a 32-point block)
+    constexpr bool wlin = (ns % 32 == 0) || (ns == 1 && 32 % r == 0);
+    constexpr int wstride = ns % 32 == 0 ? ns + ns / 32 : 1;
 #pragma unroll
     for (int b = 0; b < nb; ++b) {
         float2 x[r];
@@ -86,11 +116,11 @@ __device__ __forceinline__ void fast_stage(float2 (&v)[S::P], float2* sm, int c,
         const int j = g + S::G * b;
         const int k = j % ns;
         if constexpr (ST > 0) {
-            if (k) {
-                const int t = k * twm;
+            // w_R^(m k twm) from this stage's block: lanes with consecutive k read consecutive
+            // entries (entries with k = 0 are 1)
+            const float2* tw = twl + S::stage_off(ST) + k;
 #pragma unroll
-                for (int m = 1; m < r; ++m) x[m] = cmul(x[m], __ldg(twl + m * t));
-            }
+            for (int m = 1; m < r; ++m) x[m] = cmul(x[m], __ldg(tw + m * ns));
         }
         dft<r, float>(x);
         if constexpr (last) {
@@ -98,14 +128,26 @@ __device__ __forceinline__ void fast_stage(float2 (&v)[S::P], float2* sm, int c,
             for (int m = 0; m < r; ++m) v[b + m * nb] = x[m];
         } else {
             const int base = (j - k) * r + k;   // (j / ns) * ns * r + k
+            if constexpr (wlin) {
+                float2* w = sm + fast_addr<S>(c, base);
 #pragma unroll
-            for (int m = 0; m < r; ++m) sm[fast_addr<S>(c, base + m * ns)] = x[m];
+                for (int m = 0; m < r; ++m) w[m * wstride] = x[m];
+            } else {
+#pragma unroll
+                for (int m = 0; m < r; ++m) sm[fast_addr<S>(c, base + m * ns)] = x[m];
+            }
         }
     }
     if constexpr (!last) {
         __syncthreads();
+        if constexpr (Own<S>::linear) {
+            const float2* rd = sm + Own<S>::base(c, g);
 #pragma unroll
-        for (int i = 0; i < S::P; ++i) v[i] = sm[fast_addr<S>(c, g + S::G * i)];
+            for (int i = 0; i < S::P; ++i) v[i] = rd[Own<S>::off(i)];
+        } else {
+#pragma unroll
+            for (int i = 0; i < S::P; ++i) v[i] = sm[fast_addr<S>(c, g + S::G * i)];
+        }
         __syncthreads();
     }
 }
@@ -130,6 +172,19 @@ __device__ __forceinline__ uint64_t l2_keep_policy() {
 __device__ __forceinline__ float2 ld_table(const float2* ptr, uint64_t pol) {
     float2 v;
     asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(ptr), "l"(pol));
+    return v;
+}
+
+// Data load that reads memory only where `pred` holds and yields zero elsewhere: a predicated
+// load in inline PTX, so that the zero padding of a Bluestein input issues no memory request
+// (clamping the index to the last element made every padded load of a transform hit one L2
+// line) while all of a thread's loads stay in flight together (no branch).
+__device__ __forceinline__ float2 ld_data_if(const float2* ptr, bool pred) {
+    float2 v;
+    asm("{\n .reg .pred q;\n setp.ne.u32 q, %3, 0;\n mov.b32 %0, 0;\n mov.b32 %1, 0;\n"
+        " @q ld.global.cg.v2.f32 {%0, %1}, [%2];\n}"
+        : "=f"(v.x), "=f"(v.y)
+        : "l"(ptr), "r"((unsigned)pred));
     return v;
 }
 
@@ -169,7 +224,7 @@ __global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1)) k_fast(const __gr
     // all C columns of a tile belong to one transform (Rr is a multiple of C)
     const unsigned tile = p.reverse_tiles ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
     const Col<float> ci = make_col<float, float>(p, (int64_t)tile * C + c);
-    const float2* twl = reinterpret_cast<const float2*>(p.tw_local);
+    const float2* twl = reinterpret_cast<const float2*>(p.tw_stage);
     const int Rr = p.Rr;
     const uint64_t keep = l2_keep_policy();
 
@@ -177,24 +232,22 @@ __global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1)) k_fast(const __gr
     float2 v[P];
     const float2* src = reinterpret_cast<const float2*>(p.in) + ci.in_base + ci.jj;
     if constexpr (LD == FL_CHIRP) {
-        // Unconditional loads at indices clamped into [0, N) and a select for the zero padding:
-        // all loads of the thread are then in flight together (conditional loads were measured
-        // to serialize)
+        // predicated loads: the zero padding above N reads nothing; all loads of the thread are
+        // in flight together (branching loads were measured to serialize)
         const float2* chirp = reinterpret_cast<const float2*>(p.chirp);
         const int nlast = (int)p.nvalid - 1;
         const float2* xb = reinterpret_cast<const float2*>(p.in) + ci.in_base;
 #pragma unroll
-        for (int i = 0; i < P; ++i) v[i] = ld_data(xb + min(ci.jj + (g + G * i) * Rr, nlast));
+        for (int i = 0; i < P; ++i) {
+            const int gidx = ci.jj + (g + G * i) * Rr;
+            v[i] = ld_data_if(xb + gidx, gidx <= nlast);
+        }
         const float isign = p.conj_in ? -1.f : 1.f;
         if (p.tab_tiled) {
-            // conj(chirp) in thread order, zero above N
+            // conj(chirp) in thread order, zero above N (the padded data are zero already)
             const float2* tab = reinterpret_cast<const float2*>(p.tab_tiled) + (size_t)(ci.jj / C) * (P * S::T) + threadIdx.x;
 #pragma unroll
-            for (int i = 0; i < P; ++i) {
-                const int gidx = ci.jj + (g + G * i) * Rr;
-                const float2 u = cmul(make_float2(v[i].x, v[i].y * isign), ld_table(tab + i * S::T, keep));
-                v[i] = gidx <= nlast ? u : make_float2(0.f, 0.f);
-            }
+            for (int i = 0; i < P; ++i) v[i] = cmul(make_float2(v[i].x, v[i].y * isign), ld_table(tab + i * S::T, keep));
         } else {
 #pragma unroll
             for (int i = 0; i < P; ++i) {
@@ -209,7 +262,7 @@ __global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1)) k_fast(const __gr
 #pragma unroll
         for (int i = 0; i < P; ++i) {
             const int t = __ldg(gather + ci.jj + (g + G * i) * Rr);
-            v[i] = t >= 0 ? ld_data(base + t) : make_float2(0.f, 0.f);
+            v[i] = ld_data_if(base + t, t >= 0);
         }
         if (p.conj_in) {
 #pragma unroll
@@ -257,18 +310,31 @@ __global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1)) k_fast(const __gr
 
     // ---- store ----
     const float scale = (float)p.scale;
+    // no scaling and no conjugation (every pass but a transform's last): plain copies
+    const bool unit = p.scale == 1.0 && !p.conj_out;
     if (p.Ns_out == 1) {
         // the tile's C columns are C consecutive length-R runs of the output: flat copy
         const float sy = p.conj_out ? -scale : scale;
+        if constexpr (Own<S>::linear) {
+            float2* wr = sm + Own<S>::base(c, g);
 #pragma unroll
-        for (int i = 0; i < P; ++i) sm[fast_addr<S>(c, g + G * i)] = v[i];
+            for (int i = 0; i < P; ++i) wr[Own<S>::off(i)] = v[i];
+        } else {
+#pragma unroll
+            for (int i = 0; i < P; ++i) sm[fast_addr<S>(c, g + G * i)] = v[i];
+        }
         __syncthreads();
         const int64_t jj0 = ci.jj - c;
         float2* dst = reinterpret_cast<float2*>(p.out) + ci.out_base + jj0 * R;
+        if (unit) {
 #pragma unroll 4
-        for (int e = threadIdx.x; e < C * R; e += S::T) {
-            const float2 u = sm[fast_addr<S>(e / R, e % R)];
-            dst[e] = make_float2(u.x * scale, u.y * sy);
+            for (int e = threadIdx.x; e < C * R; e += S::T) dst[e] = sm[fast_addr<S>(e / R, e % R)];
+        } else {
+#pragma unroll 4
+            for (int e = threadIdx.x; e < C * R; e += S::T) {
+                const float2 u = sm[fast_addr<S>(e / R, e % R)];
+                dst[e] = make_float2(u.x * scale, u.y * sy);
+            }
         }
     } else {
         float2* dst = reinterpret_cast<float2*>(p.out) + ci.out_base + ci.out_j;
@@ -309,6 +375,9 @@ __global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1)) k_fast(const __gr
                     obase[t] = cscale(cadd(x0, u), scale2);
                 }
             }
+        } else if (unit) {
+#pragma unroll
+            for (int i = 0; i < P; ++i) dst[(g + G * i) * ns] = v[i];
         } else {
             const float sy = p.conj_out ? -scale : scale;
 #pragma unroll

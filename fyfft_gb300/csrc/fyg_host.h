@@ -47,6 +47,7 @@ struct TuneChoice {
     int cols = 0;
     int order = 0;       // 1: reversed pass order (the fused mid pass takes the other radix)
     int threads = 0;     // single-pass thread policy (single_pass_threads)
+    int wide = 0;        // 1: FYG_FLAG_WIDE_TILES
     double ms = 0;
 };
 bool tune_lookup(size_t n, int dtype, TuneChoice* out);

@@ -28,13 +28,14 @@ cudaError_t launch_pass(int kv, const PassParams& p, unsigned grid, int threads,
                         cudaStream_t st);
 
 // Register-resident kernels: the tile shape for R (false if R has none) and the launch.
-bool fast_shape(int R, int* C, int* threads, size_t* smem);
+bool fast_shape(int R, int wide, int* C, int* threads, size_t* smem);
 int fast_points(int R);
+int fast_stages(int R, int* radix, int* ns);   // returns the stage count (radix / ns per stage)
 cudaError_t launch_fast(const PassParams& p, unsigned grid, cudaStream_t st);
 // Thread-order tables of the register-resident kernels (kind 0: inter-pass twiddles, kind 1:
 // gather of src with optional conjugation and zero padding); see k_fast_table.
-cudaError_t launch_fast_table(float2* out, uint64_t total, int R, int kind, uint64_t Lr, uint64_t L, uint64_t Rr,
-                              const float2* src, int64_t nvalid, int conj, cudaStream_t st);
+cudaError_t launch_fast_table(float2* out, uint64_t total, int R, int wide, int kind, uint64_t Lr, uint64_t L,
+                              uint64_t Rr, const float2* src, int64_t nvalid, int conj, cudaStream_t st);
 
 // Uploads the codelet constant tables to the current device (once per device).
 cudaError_t ensure_device_constants();

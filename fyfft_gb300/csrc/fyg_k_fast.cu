@@ -14,6 +14,10 @@ cudaError_t launch_fast_2048(const PassParams& p, unsigned grid, cudaStream_t st
 cudaError_t launch_fast_4096(const PassParams& p, unsigned grid, cudaStream_t st);
 cudaError_t launch_fast_243(const PassParams& p, unsigned grid, cudaStream_t st);
 cudaError_t launch_fast_343(const PassParams& p, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_256w(const PassParams& p, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_512w(const PassParams& p, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_1024w(const PassParams& p, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_2048w(const PassParams& p, unsigned grid, cudaStream_t st);
 
 namespace {
 template <class S> bool shape_of(int* C, int* threads, size_t* smem) {
@@ -24,7 +28,16 @@ template <class S> bool shape_of(int* C, int* threads, size_t* smem) {
 }
 }  // namespace
 
-bool fast_shape(int R, int* C, int* threads, size_t* smem) {
+bool fast_shape(int R, int wide, int* C, int* threads, size_t* smem) {
+    if (wide) {
+        switch (R) {
+            case 256: return shape_of<FastR256W>(C, threads, smem);
+            case 512: return shape_of<FastR512W>(C, threads, smem);
+            case 1024: return shape_of<FastR1024W>(C, threads, smem);
+            case 2048: return shape_of<FastR2048W>(C, threads, smem);
+            default: break;   // no wide shape: the narrow one
+        }
+    }
     switch (R) {
         case 256: return shape_of<FastR256>(C, threads, smem);
         case 512: return shape_of<FastR512>(C, threads, smem);
@@ -34,6 +47,30 @@ bool fast_shape(int R, int* C, int* threads, size_t* smem) {
         case 243: return shape_of<FastR243>(C, threads, smem);
         case 343: return shape_of<FastR343>(C, threads, smem);
         default: return false;
+    }
+}
+
+namespace {
+template <class S> int stages_of(int* radix, int* ns) {
+    for (int s = 0; s < S::nst(); ++s) {
+        radix[s] = S::radix(s);
+        ns[s] = S::ns(s);
+    }
+    return S::nst();
+}
+}  // namespace
+
+// In-tile stage schedule of a register-resident tile length (the same for both widths).
+int fast_stages(int R, int* radix, int* ns) {
+    switch (R) {
+        case 256: return stages_of<FastR256>(radix, ns);
+        case 512: return stages_of<FastR512>(radix, ns);
+        case 1024: return stages_of<FastR1024>(radix, ns);
+        case 2048: return stages_of<FastR2048>(radix, ns);
+        case 4096: return stages_of<FastR4096>(radix, ns);
+        case 243: return stages_of<FastR243>(radix, ns);
+        case 343: return stages_of<FastR343>(radix, ns);
+        default: return 0;
     }
 }
 
@@ -81,17 +118,25 @@ __global__ void k_fast_table(float2* out, uint64_t total, int P, int C, int T, i
     }
 }
 
-cudaError_t launch_fast_table(float2* out, uint64_t total, int R, int kind, uint64_t Lr, uint64_t L, uint64_t Rr,
-                              const float2* src, int64_t nvalid, int conj, cudaStream_t st) {
+cudaError_t launch_fast_table(float2* out, uint64_t total, int R, int wide, int kind, uint64_t Lr, uint64_t L,
+                              uint64_t Rr, const float2* src, int64_t nvalid, int conj, cudaStream_t st) {
     int C = 0, T = 0;
     size_t smem = 0;
-    if (!fast_shape(R, &C, &T, &smem)) return cudaErrorInvalidValue;
+    if (!fast_shape(R, wide, &C, &T, &smem)) return cudaErrorInvalidValue;
     const unsigned blocks = (unsigned)std::min<uint64_t>((total + 255) / 256, 1u << 16);
     k_fast_table<<<blocks, 256, 0, st>>>(out, total, fast_points(R), C, T, kind, Lr, L, Rr, src, nvalid, conj);
     return cudaGetLastError();
 }
 
 cudaError_t launch_fast(const PassParams& p, unsigned grid, cudaStream_t st) {
+    // wide shapes are told apart by their column count
+    switch (p.g.R) {
+        case 256: if (p.g.C == FastR256W::C) return launch_fast_256w(p, grid, st); break;
+        case 512: if (p.g.C == FastR512W::C) return launch_fast_512w(p, grid, st); break;
+        case 1024: if (p.g.C == FastR1024W::C) return launch_fast_1024w(p, grid, st); break;
+        case 2048: if (p.g.C == FastR2048W::C) return launch_fast_2048w(p, grid, st); break;
+        default: break;
+    }
     switch (p.g.R) {
         case 256: return launch_fast_256(p, grid, st);
         case 512: return launch_fast_512(p, grid, st);

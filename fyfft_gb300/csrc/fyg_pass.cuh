@@ -105,6 +105,10 @@ struct alignas(16) PassParams {
     // register-resident kernels: 1 = tiles in reverse order (odd passes of a pipeline start on
     // the tail the previous pass left in L2)
     int reverse_tiles;
+    // register-resident kernels: in-tile stage twiddles, one block per stage s >= 1 holding
+    // w_R^(m k twm_s) at m ns_s + k (m < radix, k < ns_s), so that the lanes of a warp (consecutive
+    // k for a fixed m) read consecutive entries
+    const void* tw_stage;
 };
 
 __device__ __forceinline__ int64_t transform_base(const int64_t* offs, const int* ids, int64_t b, int64_t dist) {

@@ -610,14 +610,42 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
         // register-resident kernel for the tile lengths it is compiled for (FP32; not for the
         // tiles of uneven batches, which run inside the generic persistent kernel); the
         // inter-pass twiddle table needs C | Ns
-        int fc = 0, ft = 0;
+        int fc = 0, ft = 0, wide = 0;
         size_t fsm = 0;
-        if (pl->dtype == FYG_C32 && cb == 8 && !single &&
-            !(pl->flags & (FYG_FLAG_SMALL_TILES | FYG_FLAG_GENERIC_KERNELS)) && fast_shape(R, &fc, &ft, &fsm) &&
-            (L / R) % (uint64_t)fc == 0 && !(p.mid && (p.load_mode != LD_PLAIN || p.Ns <= 1)) &&
-            (p.Ns <= 1 || p.Ns % fc == 0)) {
+        auto shape_ok = [&](int w) {
+            return fast_shape(R, w, &fc, &ft, &fsm) && (L / R) % (uint64_t)fc == 0 && (p.Ns <= 1 || p.Ns % fc == 0);
+        };
+        // the wide shape (FYG_FLAG_WIDE_TILES) where its column count divides the pass, else
+        // the narrow one
+        const bool want_fast = pl->dtype == FYG_C32 && cb == 8 && !single &&
+                               !(pl->flags & (FYG_FLAG_SMALL_TILES | FYG_FLAG_GENERIC_KERNELS)) &&
+                               !(p.mid && (p.load_mode != LD_PLAIN || p.Ns <= 1));
+        bool fast = false;
+        if (want_fast && (pl->flags & FYG_FLAG_WIDE_TILES) && shape_ok(1)) { fast = true; wide = 1; }
+        else if (want_fast && shape_ok(0)) fast = true;
+        if (fast) {
             fill_geom(p.g, R, fc, false, rad);
             p.reverse_tiles = i & 1;   // measured 0.3-2% faster than one order for all passes
+            // in-tile stage twiddles, one block per stage s >= 1: w_R^(m k twm) at m ns + k
+            {
+                int srad[kMaxStages], sns[kMaxStages];
+                const int nst = fast_stages(R, srad, sns);
+                int rc = cached_table(pl, "stagetw:" + std::to_string(R), [&](DevBuf& b) {
+                    std::vector<float2> t;
+                    for (int st = 1; st < nst; ++st) {
+                        const uint64_t twm = (uint64_t)R / ((uint64_t)sns[st] * (uint64_t)srad[st]);
+                        for (int m = 0; m < srad[st]; ++m)
+                            for (int k = 0; k < sns[st]; ++k) {
+                                long double c, sn;
+                                twiddle_ld((uint64_t)m * (uint64_t)k * twm, (uint64_t)R, &c, &sn);
+                                t.push_back(make_float2((float)c, (float)sn));
+                            }
+                    }
+                    if (t.empty()) t.push_back(make_float2(1.f, 0.f));
+                    return b.upload(t.data(), t.size() * sizeof(float2));
+                }, &p.tw_stage);
+                if (rc) return rc;
+            }
             d.kv = KV_FAST;
             d.threads = ft;
             d.smem = fsm;
@@ -629,14 +657,15 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
                 return cached_table(pl, "tiled:" + key, [&](DevBuf& b) {
                     int rc = b.alloc(total * sizeof(float2));
                     if (rc) return rc;
-                    cudaError_t e = launch_fast_table(static_cast<float2*>(b.ptr), total, R, kind, (uint64_t)p.Lr, L,
-                                                      (uint64_t)p.Rr, static_cast<const float2*>(src), nvalid, conj, 0);
+                    cudaError_t e = launch_fast_table(static_cast<float2*>(b.ptr), total, R, wide, kind, (uint64_t)p.Lr,
+                                                      L, (uint64_t)p.Rr, static_cast<const float2*>(src), nvalid, conj,
+                                                      0);
                     if (e == cudaSuccess) e = cudaStreamSynchronize(0);
                     return e == cudaSuccess ? FYG_OK : cuda_error(e, "thread-order table");
                 }, outp);
             };
-            const std::string sh = std::to_string(R) + ":" + std::to_string(Ns) + ":" + std::to_string(L) + ":" +
-                                   ct.src_key;
+            const std::string sh = std::to_string(R) + "x" + std::to_string(fc) + ":" + std::to_string(Ns) + ":" +
+                                   std::to_string(L) + ":" + ct.src_key;
             int rc = FYG_OK;
             if (p.Ns > 1 && p.load_mode == LD_PLAIN) {
                 rc = tiled("tw:" + sh, Ns * (uint64_t)R, 0, nullptr, 0, 0, &p.tw_tiled);
@@ -1192,8 +1221,8 @@ int fyg_plan_create(size_t n, int dtype, size_t batch, int flags, fyg_plan** out
     if (flags & FYG_FLAG_AUTOTUNED) {
         TuneChoice tc;
         if (tune_lookup(n, dtype, &tc))
-            return plan_create_opts(n, dtype, batch, flags, tc.max_pass_radix, tc.conv_length, tc.cols, tc.order,
-                                    tc.threads, out);
+            return plan_create_opts(n, dtype, batch, flags | (tc.wide ? FYG_FLAG_WIDE_TILES : 0), tc.max_pass_radix,
+                                    tc.conv_length, tc.cols, tc.order, tc.threads, out);
         flags &= ~FYG_FLAG_AUTOTUNED;
     }
     if (!out) return set_error(FYG_ERR_NULL_PTR, "out is null");

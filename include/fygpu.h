@@ -58,6 +58,9 @@ extern "C" {
 #define FYG_FLAG_AUTOTUNED 0x10  /* use the autotuner's cached schedule for this length, if any */
 #define FYG_FLAG_GENERIC_KERNELS 0x20 /* only the generic tile kernel (no register-resident
                                        * power-of-two kernels); for comparisons */
+#define FYG_FLAG_WIDE_TILES 0x40 /* register-resident passes in 512-thread CTAs with twice the
+                                  * columns (wider contiguous row segments); chosen per length by
+                                  * the autotuner */
 
 typedef struct fyg_plan fyg_plan;
 typedef struct fyg_batch fyg_batch;

@@ -41,8 +41,8 @@ def test_cache_file_lists_every_length(cache):
     assert doc["device"] and torch.cuda.get_device_name(0) in doc["device"]
     for n in LENGTHS:
         e = doc["entries"][f"c32:{n}"]
-        assert e["ms"] > 0 and set(e) == {"max_pass_radix", "conv_length", "cols", "order", "threads", "ms"}
-        assert e["threads"] in (0, 1)
+        assert e["ms"] > 0 and set(e) == {"max_pass_radix", "conv_length", "cols", "order", "threads", "wide", "ms"}
+        assert e["threads"] in (0, 1) and e["wide"] in (0, 1)
 
 
 @pytest.mark.parametrize("n", LENGTHS)
@@ -84,7 +84,7 @@ def test_cache_for_another_device_is_ignored(tmp_path):
     with open(path, "w") as f:
         f.write('{\n  "device": "some other GPU|1|1.0|1",\n  "entries": {\n'
                 '    "c32:1009": {"max_pass_radix": 0, "conv_length": 5000, "cols": 0, "order": 0, "threads": 0, '
-                '"ms": 1.0}\n  }\n}\n')
+                '"wide": 0, "ms": 1.0}\n  }\n}\n')
     # tuning another length into that file replaces the foreign entries
     fg.autotune(2520, "complex64", 4, cache_path=path)
     doc = json.load(open(path))

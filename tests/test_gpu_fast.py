@@ -107,3 +107,21 @@ def test_bluestein_on_243_tiles(inverse):
     assert kernels(p) == ["fast"] * 3, p.describe()
     for b in range(3):
         assert O.rel_l2(y[b], O.fft(x[b], inverse=inverse)) <= 2e-6
+
+
+# wide tiles (FYG_FLAG_WIDE_TILES): 512-thread CTAs with twice the columns, every fusion
+@pytest.mark.parametrize("n,batch", [(1 << 16, 8), (1 << 18, 4), (1 << 20, 2), (1 << 21, 2), (65537, 3),
+                                     (131074, 2), (999983, 2)])
+@pytest.mark.parametrize("inverse", [False, True])
+def test_wide_tiles(n, batch, inverse):
+    p, x, y = run(n, batch, inverse, flags=fg.FYG_FLAG_WIDE_TILES)
+    desc = p.describe()
+    assert "fast" in kernels(p)
+    # at least one pass runs a wide shape (C of 8 at 2048, 16 at 1024, 32 at 512 and 256)
+    wide_c = {"2048": "8", "1024": "16", "512": "32", "256": "32"}
+    assert any(f"R={r} C={c} " in ln for ln in desc for r, c in wide_c.items()), desc
+    _, _, yn = run(n, batch, inverse)
+    for b in (0, batch - 1):
+        ref = O.fft(x[b], inverse=inverse)
+        assert O.rel_l2(y[b], ref) <= 2e-6 and O.rel_l2(y[b], ref) <= 4 * np.log2(n) * EPS32
+        assert O.rel_l2(y[b], yn[b]) <= 2e-7
