@@ -30,7 +30,7 @@ FYG_C32, FYG_C64 = 0, 1
 FYG_FORWARD, FYG_INVERSE = 1, -1
 FYG_FLAG_CONV_FP64, FYG_FLAG_CONV_FP32, FYG_FLAG_NO_L2_CHUNK = 1, 2, 4
 FYG_FLAG_SMALL_TILES, FYG_FLAG_AUTOTUNED, FYG_FLAG_GENERIC_KERNELS = 8, 16, 32
-FYG_FLAG_WIDE_TILES = 64
+FYG_FLAG_WIDE_TILES, FYG_FLAG_TMA_LOADS, FYG_FLAG_NO_TMA_LOADS = 64, 128, 256
 
 # every symbol include/fygpu.h declares
 EXPORTED_SYMBOLS = (
@@ -43,6 +43,7 @@ EXPORTED_SYMBOLS = (
     "fyg_fill_random_device", "fyg_version", "fyg_plan_cache_stats", "fyg_plan_cache_clear",
     "fyg_partition", "fyg_multi_create", "fyg_multi_shards", "fyg_multi_execute", "fyg_multi_execute_device",
     "fyg_multi_synchronize", "fyg_multi_destroy", "fyg_fill_random_at", "fyg_fill_random_device_at",
+    "fyg_plan_status",
 )
 
 
@@ -104,6 +105,7 @@ def lib() -> ctypes.CDLL:
         L.fyg_plan_cache_stats.argtypes = [ctypes.POINTER(sz), ctypes.POINTER(sz), ctypes.POINTER(u64),
                                            ctypes.POINTER(u64)]
         L.fyg_partition.argtypes = [ctypes.POINTER(sz), sz, i, ctypes.POINTER(sz)]
+        L.fyg_plan_status.argtypes = [vp, vp, ctypes.POINTER(i)]
         L.fyg_multi_create.argtypes = [sz, i, sz, i, ctypes.POINTER(i), i, ctypes.POINTER(vp)]
         L.fyg_multi_shards.argtypes = [vp, ctypes.POINTER(i), ctypes.POINTER(sz)]
         L.fyg_multi_execute.argtypes = [vp, vp, vp, i]
@@ -271,6 +273,12 @@ class FFT1D_C2C_invoker:
         """output = scale * F^H g (= scale * N * backward(g))."""
         px, py = self._io(g, output)
         check(lib().fyg_execute_adjoint(self._h, px, py, float(scale), _stream_handle(stream)))
+
+    def status(self, stream=None) -> int:
+        """Device error bits recorded by the plan's kernels since the last call (0 = none)."""
+        st = ctypes.c_int()
+        check(lib().fyg_plan_status(self._h, _stream_handle(stream), ctypes.byref(st)))
+        return st.value
 
     def info(self):
         L, P, S = ctypes.c_size_t(), ctypes.c_int(), ctypes.c_int()

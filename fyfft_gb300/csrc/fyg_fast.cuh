@@ -24,6 +24,8 @@
 // conjugation, the Bluestein output chirp with truncation or the Rader scatter with the x0 and
 // DC terms at the store.  Uneven batches use the generic kernel (fyg_kernels.cuh).
 #pragma once
+#include <cuda.h>   // CUtensorMap (an opaque, 64-byte aligned descriptor passed by value)
+
 #include "fyg_pass.cuh"
 
 namespace fyg {
@@ -188,6 +190,46 @@ __device__ __forceinline__ float2 ld_data_if(const float2* ptr, bool pred) {
     return v;
 }
 
+// ---- TMA tile loads (cp.async.bulk.tensor) ----
+// One thread arms an mbarrier with the tile's byte count and issues the 2D tensor loads of the
+// C columns x R rows of the tile (boxes of 2C floats x 256 rows) into shared memory; every thread
+// waits on the barrier's phase.  The wait is bounded (globaltimer, 2 s): on expiry the kernel
+// records an error bit and carries on with whatever the buffer holds, so no thread leaves a
+// barrier the others still reach.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t mb, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mb), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mb, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t mb) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(mb)
+        : "memory");
+}
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mb, uint32_t parity) {
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred q;\n mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n selp.u32 %0, 1, 0, q;\n}"
+            : "=r"(done)
+            : "r"(mb), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (global_ns() - t0 > 2000000000ull) return false;
+    }
+}
+
 // Load variants, compiled as separate kernels so that each gets its own register allocation.
 enum FastLoad : int {
     FL_PLAIN = 0,     // x (conjugated for inverses): first passes
@@ -214,9 +256,12 @@ __device__ __forceinline__ void fast_twiddle(float2 (&v)[P], const PassParams& p
     }
 }
 
-template <class S, int LD, bool MID>
-__global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1)) k_fast(const __grid_constant__ PassParams p) {
-    extern __shared__ __align__(16) unsigned char smraw[];
+// TMA: the data of a FL_PLAIN / FL_TWIDDLE load arrive by tensor copies (tmap describes the pass
+// input as rows of 2 Rr floats, one row per point of a transform) instead of per-thread loads.
+template <class S, int LD, bool MID, bool TMA = false>
+__global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1))
+    k_fast(const __grid_constant__ PassParams p, const __grid_constant__ CUtensorMap tmap) {
+    extern __shared__ __align__(128) unsigned char smraw[];
     float2* sm = reinterpret_cast<float2*>(smraw);
     constexpr int P = S::P, G = S::G, C = S::C, R = S::R;
     const int c = threadIdx.x % C;
@@ -271,8 +316,32 @@ __global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1)) k_fast(const __gr
         if (p.x0_from_in && p.x0buf && ci.jj == 0 && g == 0)
             reinterpret_cast<float2*>(p.x0buf)[ci.b] = ld_data(base);
     } else {
+        if constexpr (TMA) {
+            // the tile lands in the exchange buffer as [point][column] (C float2 per row), so
+            // that thread (c, g) reads point g + G i at (g + G i) C + c: consecutive threads,
+            // consecutive words
+            static_assert(R % 256 == 0 || R < 256, "TMA boxes hold 256 rows");
+            constexpr int box_rows = R < 256 ? R : 256;
+            __shared__ __align__(8) uint64_t mbar;
+            const uint32_t mb = smem_u32(&mbar);
+            if (threadIdx.x == 0) mbar_init(mb, 1);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                mbar_expect_tx(mb, (uint32_t)(C * R * sizeof(float2)));
+                const int x = 2 * (ci.jj - c);      // first column of the tile, in floats
+                const int y = ci.b * R;             // first row: point 0 of this transform
+#pragma unroll 1
+                for (int k = 0; k < R / box_rows; ++k)
+                    tma_load_2d(smem_u32(sm + (size_t)k * box_rows * C), &tmap, x, y + k * box_rows, mb);
+            }
+            if (!mbar_wait_bounded(mb, 0) && p.err) atomicOr(p.err, 4);
 #pragma unroll
-        for (int i = 0; i < P; ++i) v[i] = ld_data(src + (g + G * i) * Rr);
+            for (int i = 0; i < P; ++i) v[i] = sm[(g + G * i) * C + c];
+            __syncthreads();   // the buffer is the exchange buffer of the first stage
+        } else {
+#pragma unroll
+            for (int i = 0; i < P; ++i) v[i] = ld_data(src + (g + G * i) * Rr);
+        }
         if (p.conj_in) {
 #pragma unroll
             for (int i = 0; i < P; ++i) v[i].y = -v[i].y;

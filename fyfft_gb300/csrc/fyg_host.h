@@ -93,6 +93,8 @@ struct PassDesc {
     int threads;
     size_t smem;
     int64_t in_elem_bytes, out_elem_bytes;
+    bool tma = false;      // register-resident pass whose input arrives by TMA tile loads
+    CUtensorMap tmap;      // (FYG_FLAG_TMA_LOADS; the input is a scratch buffer of the plan)
 };
 
 // Process-wide cache of read-only plan tables (twiddles, chirps, Rader index maps, convolution

@@ -1,5 +1,6 @@
 // fyg_internal.h -- host-side declarations shared by the library's translation units.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -25,13 +26,15 @@ VariantInfo variant_info(int kv);
 
 // Launches one tile pass; sets the dynamic shared-memory attribute when needed.
 cudaError_t launch_pass(int kv, const PassParams& p, unsigned grid, int threads, size_t smem,
-                        cudaStream_t st);
+                        cudaStream_t st, const CUtensorMap* tmap = nullptr);
 
 // Register-resident kernels: the tile shape for R (false if R has none) and the launch.
 bool fast_shape(int R, int wide, int* C, int* threads, size_t* smem);
 int fast_points(int R);
 int fast_stages(int R, int* radix, int* ns);   // returns the stage count (radix / ns per stage)
-cudaError_t launch_fast(const PassParams& p, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast(const PassParams& p, const CUtensorMap* tmap, unsigned grid, cudaStream_t st);
+// Tensor map of a register-resident pass input for TMA tile loads (fyg_k_fast.cu).
+cudaError_t encode_tile_map(CUtensorMap* map, const void* base, uint64_t Rr, uint64_t rows, int C, int R);
 // Thread-order tables of the register-resident kernels (kind 0: inter-pass twiddles, kind 1:
 // gather of src with optional conjugation and zero padding); see k_fast_table.
 cudaError_t launch_fast_table(float2* out, uint64_t total, int R, int wide, int kind, uint64_t Lr, uint64_t L,

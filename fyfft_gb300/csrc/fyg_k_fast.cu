@@ -3,21 +3,24 @@
 #include "fyg_internal.h"
 #include "fyg_fast.cuh"
 
+#include <cudaTypedefs.h>
+
 #include <algorithm>
+#include <mutex>
 
 namespace fyg {
 
-cudaError_t launch_fast_256(const PassParams& p, unsigned grid, cudaStream_t st);
-cudaError_t launch_fast_512(const PassParams& p, unsigned grid, cudaStream_t st);
-cudaError_t launch_fast_1024(const PassParams& p, unsigned grid, cudaStream_t st);
-cudaError_t launch_fast_2048(const PassParams& p, unsigned grid, cudaStream_t st);
-cudaError_t launch_fast_4096(const PassParams& p, unsigned grid, cudaStream_t st);
-cudaError_t launch_fast_243(const PassParams& p, unsigned grid, cudaStream_t st);
-cudaError_t launch_fast_343(const PassParams& p, unsigned grid, cudaStream_t st);
-cudaError_t launch_fast_256w(const PassParams& p, unsigned grid, cudaStream_t st);
-cudaError_t launch_fast_512w(const PassParams& p, unsigned grid, cudaStream_t st);
-cudaError_t launch_fast_1024w(const PassParams& p, unsigned grid, cudaStream_t st);
-cudaError_t launch_fast_2048w(const PassParams& p, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_256(const PassParams& p, const CUtensorMap* tmap, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_512(const PassParams& p, const CUtensorMap* tmap, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_1024(const PassParams& p, const CUtensorMap* tmap, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_2048(const PassParams& p, const CUtensorMap* tmap, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_4096(const PassParams& p, const CUtensorMap* tmap, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_243(const PassParams& p, const CUtensorMap* tmap, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_343(const PassParams& p, const CUtensorMap* tmap, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_256w(const PassParams& p, const CUtensorMap* tmap, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_512w(const PassParams& p, const CUtensorMap* tmap, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_1024w(const PassParams& p, const CUtensorMap* tmap, unsigned grid, cudaStream_t st);
+cudaError_t launch_fast_2048w(const PassParams& p, const CUtensorMap* tmap, unsigned grid, cudaStream_t st);
 
 namespace {
 template <class S> bool shape_of(int* C, int* threads, size_t* smem) {
@@ -128,23 +131,52 @@ cudaError_t launch_fast_table(float2* out, uint64_t total, int R, int wide, int 
     return cudaGetLastError();
 }
 
-cudaError_t launch_fast(const PassParams& p, unsigned grid, cudaStream_t st) {
+// Tensor map of a pass input for the TMA loads: rows of 2 Rr floats (the Rr columns of one point
+// index of one transform), `rows` rows (transforms x R), boxes of 2C floats x min(R, 256) rows.
+// cuTensorMapEncodeTiled comes from the driver through the runtime's entry-point query (no
+// link against the driver library).
+cudaError_t encode_tile_map(CUtensorMap* map, const void* base, uint64_t Rr, uint64_t rows, int C, int R) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        else
+            cudaGetLastError();
+    });
+    if (!encode) return cudaErrorNotSupported;
+    if ((reinterpret_cast<uintptr_t>(base) & 15) || ((Rr * 8) & 15)) return cudaErrorInvalidValue;
+    const cuuint64_t dims[2] = {2 * Rr, rows};
+    const cuuint64_t strides[1] = {Rr * sizeof(float2)};
+    const cuuint32_t box[2] = {(cuuint32_t)(2 * C), (cuuint32_t)std::min(R, 256)};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box,
+                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+cudaError_t launch_fast(const PassParams& p, const CUtensorMap* tmap, unsigned grid, cudaStream_t st) {
     // wide shapes are told apart by their column count
     switch (p.g.R) {
-        case 256: if (p.g.C == FastR256W::C) return launch_fast_256w(p, grid, st); break;
-        case 512: if (p.g.C == FastR512W::C) return launch_fast_512w(p, grid, st); break;
-        case 1024: if (p.g.C == FastR1024W::C) return launch_fast_1024w(p, grid, st); break;
-        case 2048: if (p.g.C == FastR2048W::C) return launch_fast_2048w(p, grid, st); break;
+        case 256: if (p.g.C == FastR256W::C) return launch_fast_256w(p, tmap, grid, st); break;
+        case 512: if (p.g.C == FastR512W::C) return launch_fast_512w(p, tmap, grid, st); break;
+        case 1024: if (p.g.C == FastR1024W::C) return launch_fast_1024w(p, tmap, grid, st); break;
+        case 2048: if (p.g.C == FastR2048W::C) return launch_fast_2048w(p, tmap, grid, st); break;
         default: break;
     }
     switch (p.g.R) {
-        case 256: return launch_fast_256(p, grid, st);
-        case 512: return launch_fast_512(p, grid, st);
-        case 1024: return launch_fast_1024(p, grid, st);
-        case 2048: return launch_fast_2048(p, grid, st);
-        case 4096: return launch_fast_4096(p, grid, st);
-        case 243: return launch_fast_243(p, grid, st);
-        case 343: return launch_fast_343(p, grid, st);
+        case 256: return launch_fast_256(p, tmap, grid, st);
+        case 512: return launch_fast_512(p, tmap, grid, st);
+        case 1024: return launch_fast_1024(p, tmap, grid, st);
+        case 2048: return launch_fast_2048(p, tmap, grid, st);
+        case 4096: return launch_fast_4096(p, tmap, grid, st);
+        case 243: return launch_fast_243(p, tmap, grid, st);
+        case 343: return launch_fast_343(p, tmap, grid, st);
         default: return cudaErrorInvalidValue;
     }
 }

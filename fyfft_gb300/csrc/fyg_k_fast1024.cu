@@ -1,7 +1,7 @@
 // Register-resident kernels of tile length 1024 (all load variants).
 #include "fyg_k_fast.cuh"
 namespace fyg {
-cudaError_t launch_fast_1024(const PassParams& p, unsigned grid, cudaStream_t st) {
-    return launch_fast_shape<FastR1024>(p, grid, st);
+cudaError_t launch_fast_1024(const PassParams& p, const CUtensorMap* tmap, unsigned grid, cudaStream_t st) {
+    return launch_fast_shape<FastR1024>(p, tmap, grid, st);
 }
 }  // namespace fyg

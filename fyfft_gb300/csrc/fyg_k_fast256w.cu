@@ -1,7 +1,7 @@
 // Register-resident kernels of tile length 256, wide shape (512 threads, all load variants).
 #include "fyg_k_fast.cuh"
 namespace fyg {
-cudaError_t launch_fast_256w(const PassParams& p, unsigned grid, cudaStream_t st) {
-    return launch_fast_shape<FastR256W>(p, grid, st);
+cudaError_t launch_fast_256w(const PassParams& p, const CUtensorMap* tmap, unsigned grid, cudaStream_t st) {
+    return launch_fast_shape<FastR256W>(p, tmap, grid, st);
 }
 }  // namespace fyg

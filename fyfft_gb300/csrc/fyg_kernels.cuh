@@ -44,7 +44,8 @@ template <bool COLMAJOR> struct Lay {
 // iteration (operands in registers), so register use depends only on the radix.
 template <typename T, int RADIX, bool COLMAJOR>
 __device__ __forceinline__ void stage_pp(const cplx<T>* src, cplx<T>* dst, const Lay<COLMAJOR> L, int R,
-                                         FastDiv nsd, FastDiv rrd, int twm, const cplx<T>* twl) {
+                                         FastDiv nsd, FastDiv rrd, int twm, const cplx<T>* twl,
+                                         const cplx<T>* twst) {
     using T2 = cplx<T>;
     const int Rr_l = R / RADIX;
     const int total = Rr_l * L.C;
@@ -67,9 +68,18 @@ __device__ __forceinline__ void stage_pp(const cplx<T>* src, cplx<T>* dst, const
         const int q = (int)nsd.div((uint32_t)j);
         const int k = j - q * ns;
         if (k) {
-            const int t = k * twm;
+            if (twst) {
+                // the stage's block of the stage-twiddle table: w_R^(m k twm) at m ns + k, so
+                // that threads with consecutive k (consecutive butterflies) read consecutive
+                // entries
+                const cplx<T>* tw = twst + k;
 #pragma unroll
-            for (int m = 1; m < RADIX; ++m) v[m] = cmul(v[m], __ldg(twl + m * t));
+                for (int m = 1; m < RADIX; ++m) v[m] = cmul(v[m], __ldg(tw + m * ns));
+            } else {
+                const int t = k * twm;
+#pragma unroll
+                for (int m = 1; m < RADIX; ++m) v[m] = cmul(v[m], __ldg(twl + m * t));
+            }
         }
         dft<RADIX, T>(v);
         const int base = q * ns * RADIX + k;
@@ -91,17 +101,19 @@ template <typename T, int CLASS, bool COLMAJOR>
 __device__ __forceinline__ int run_stages(const PassParams& p, const StageDesc* sd, cplx<T>* const* bufs, int w,
                                           const Lay<COLMAJOR> L) {
     const cplx<T>* twl = reinterpret_cast<const cplx<T>*>(p.tw_local);
+    const cplx<T>* twst = reinterpret_cast<const cplx<T>*>(p.tw_stage);
     const int nst = p.g.nst, R = p.g.R;
     for (int s = 0; s < nst; ++s) {
         const StageDesc d = sd[s];
+        const cplx<T>* tws = twst ? twst + d.twoff : nullptr;
         const cplx<T>* src = bufs[w];
         cplx<T>* dst = bufs[w ^ 1];
         switch (d.radix) {
-#define FYG_CASE(r) case r: stage_pp<T, r, COLMAJOR>(src, dst, L, R, d.ns, d.rr, d.twm, twl); break;
+#define FYG_CASE(r) case r: stage_pp<T, r, COLMAJOR>(src, dst, L, R, d.ns, d.rr, d.twm, twl, tws); break;
             FYG_RADICES_C16(FYG_CASE)
 #undef FYG_CASE
 #define FYG_CASE(r) \
-    case r: if constexpr (CLASS >= 32) stage_pp<T, r, COLMAJOR>(src, dst, L, R, d.ns, d.rr, d.twm, twl); break;
+    case r: if constexpr (CLASS >= 32) stage_pp<T, r, COLMAJOR>(src, dst, L, R, d.ns, d.rr, d.twm, twl, tws); break;
             FYG_RADICES_C32_ONLY(FYG_CASE)
 #undef FYG_CASE
             default:
@@ -415,7 +427,13 @@ __device__ __forceinline__ void tile_body(const PassParams& p, int64_t tile, uns
         // unrolled selects keep the parameter reads at constant offsets
 #pragma unroll
         for (int t = 0; t < kMaxStages; ++t)
-            if (t == s) { d.radix = p.g.radix[t]; d.twm = p.g.twmul[t]; d.ns = p.g.ns[t]; d.rr = p.g.rr[t]; }
+            if (t == s) {
+                d.radix = p.g.radix[t];
+                d.twm = p.g.twmul[t];
+                d.twoff = p.g.twoff[t];
+                d.ns = p.g.ns[t];
+                d.rr = p.g.rr[t];
+            }
         sd[s] = d;
     }
     const bool need_head = !(plain_out && (flat_out || !COLMAJOR)) || p.x0_from_in;

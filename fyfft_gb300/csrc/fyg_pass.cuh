@@ -51,6 +51,7 @@ struct TileGeom {
     int nst;        // in-CTA stages
     int radix[kMaxStages];
     int twmul[kMaxStages];     // R / (ns * radix): local twiddle exponent multiplier
+    int twoff[kMaxStages];     // offset of the stage's block in the stage-twiddle table
     FastDiv ns[kMaxStages];    // local Ns before the stage
     FastDiv rr[kMaxStages];    // R / radix (butterflies per column)
     FastDiv divR;              // R (element index -> column, column-major order)
@@ -147,7 +148,7 @@ template <typename T> struct ColHead {
 // Stage schedule copied to shared memory at kernel start (parameter arrays cannot be indexed
 // by a run-time stage number without a local-memory copy).
 struct StageDesc {
-    int radix, twm;
+    int radix, twm, twoff;
     FastDiv ns, rr;
 };
 

@@ -46,8 +46,9 @@ VariantInfo variant_info(int kv) {
     return {512, (kv == KV_F32_C16 || kv == KV_F32_C32 || kv == KV_FAST) ? 8 : 16};
 }
 
-cudaError_t launch_pass(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st) {
-    if (kv == KV_FAST) return launch_fast(p, grid, st);
+cudaError_t launch_pass(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st,
+                        const CUtensorMap* tmap) {
+    if (kv == KV_FAST) return launch_fast(p, tmap, grid, st);
     if (kv == KV_F32_C16) return launch_f32(kv, p, grid, threads, smem, st);
     if (kv == KV_F32_C32) return launch_f32c32(kv, p, grid, threads, smem, st);
     if (kv == KV_F64_C16) return launch_f64(kv, p, grid, threads, smem, st);
@@ -368,12 +369,14 @@ void fill_geom(TileGeom& g, int R, int C, bool colmajor, const std::vector<int>&
     g.log2C = lc;
     g.colmajor = colmajor ? 1 : 0;
     g.nst = (int)rad.size();
-    int ns = 1;
+    int ns = 1, off = 0;
     for (size_t s = 0; s < rad.size(); ++s) {
         g.radix[s] = rad[s];
         g.ns[s] = make_fastdiv((uint32_t)ns);
         g.twmul[s] = R / (ns * rad[s]);
         g.rr[s] = make_fastdiv((uint32_t)(R / rad[s]));
+        g.twoff[s] = off;                       // stage 0 has no twiddles and no block
+        if (s > 0) off += rad[s] * ns;
         ns *= rad[s];
     }
     g.divR = make_fastdiv((uint32_t)R);
@@ -552,6 +555,39 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
         const int C = single ? ps.C : multi_C(cb, R);
         const std::vector<int> rad = radices_for(R, cb);
         fill_geom(p.g, R, C, single, rad);
+        // stage twiddles of the tile kernel's in-CTA schedule, one block per stage s >= 1:
+        // w_R^(m k twm_s) at twoff_s + m ns_s + k
+        {
+            std::string key = "gstage:" + std::to_string(R) + ":" + std::to_string(cb);
+            for (int r : rad) key += ":" + std::to_string(r);
+            int rc = cached_table(pl, key, [&](DevBuf& b) {
+                std::vector<unsigned char> t;
+                uint64_t ns = 1;
+                auto put = [&](long double c, long double sn) {
+                    if (cb == 8) {
+                        const float2 v = make_float2((float)c, (float)sn);
+                        t.insert(t.end(), (const unsigned char*)&v, (const unsigned char*)&v + sizeof(v));
+                    } else {
+                        const double2 v = make_double2((double)c, (double)sn);
+                        t.insert(t.end(), (const unsigned char*)&v, (const unsigned char*)&v + sizeof(v));
+                    }
+                };
+                for (size_t st = 0; st < rad.size(); ++st) {
+                    const uint64_t r = (uint64_t)rad[st], twm = (uint64_t)R / (ns * r);
+                    if (st > 0)
+                        for (uint64_t m = 0; m < r; ++m)
+                            for (uint64_t k = 0; k < ns; ++k) {
+                                long double c, sn;
+                                twiddle_ld(m * k * twm, (uint64_t)R, &c, &sn);
+                                put(c, sn);
+                            }
+                    ns *= r;
+                }
+                if (t.empty()) put(1.0L, 0.0L);
+                return b.upload(t.data(), t.size());
+            }, &p.tw_stage);
+            if (rc) return rc;
+        }
         p.Rr = (int)(L / R);
         p.Ns = (int)Ns;
         p.Ns_out = mid ? 1 : (int)Ns;
@@ -676,6 +712,23 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
             else if (!rc && p.store_mode == ST_CHIRP && p.Ns_out == p.Rr)
                 rc = tiled("chout:" + sh, L, 1, ct.chirp, (int64_t)n, 0, &p.tab_tiled);
             if (rc) return rc;
+        }
+        // TMA tile loads for register-resident passes that read a scratch buffer of the plan
+        // (its address is fixed; power-of-two tiles, boxes of 256 rows).  By default only for
+        // tiles of 4 columns (32-byte rows: R = 2048, 4096), where they measured faster than
+        // per-thread loads (Bluestein 999983 x 64 mid pass 0.809 -> 0.733 ms); on 8-column tiles
+        // they measured slower (2^20 x 64 second pass 0.216 -> 0.240 ms).
+        // FYG_FLAG_TMA_LOADS: every eligible pass; FYG_FLAG_NO_TMA_LOADS: none.
+        const bool tma_wanted = !(pl->flags & FYG_FLAG_NO_TMA_LOADS) &&
+                                ((pl->flags & FYG_FLAG_TMA_LOADS) || (d.kv == KV_FAST && p.g.C <= 4));
+        if (tma_wanted && d.kv == KV_FAST && p.load_mode == LD_PLAIN && p.Ns > 1 &&
+            (d.in_role == ROLE_S0 || d.in_role == ROLE_S1) && (R % 256 == 0)) {
+            const void* base = d.in_role == ROLE_S0 ? pl->scratch0.ptr : pl->scratch1.ptr;
+            if (encode_tile_map(&d.tmap, base, (uint64_t)p.Rr, (uint64_t)pl->chunk * (uint64_t)R, p.g.C, R) ==
+                cudaSuccess)
+                d.tma = true;
+            else
+                cudaGetLastError();
         }
         if (d.smem > kSmemLimit)
             return set_error(FYG_ERR_UNSUPPORTED, "tile of " + std::to_string(R) + "x" + std::to_string(C) +
@@ -957,7 +1010,7 @@ static int run_pipeline(fyg_plan* pl, const std::vector<PassDesc>& pipe, const v
                 e1 = pl->prof_pool[pl->prof_pool_used++];
                 cudaEventRecord(e0, st);
             }
-            cudaError_t e = launch_pass(d.kv, p, grid, d.threads, d.smem, st);
+            cudaError_t e = launch_pass(d.kv, p, grid, d.threads, d.smem, st, d.tma ? &d.tmap : nullptr);
             if (e != cudaSuccess) return cuda_error(e, "tile pass launch");
             if (e0) {
                 cudaEventRecord(e1, st);
@@ -1366,6 +1419,22 @@ int fyg_plan_cache_clear(void) {
         if (it->second.use_count() == 1) it = tc.map.erase(it);   // no live plan holds it
         else ++it;
     }
+    return FYG_OK;
+}
+
+int fyg_plan_status(fyg_plan* plan, void* stream, int* status) {
+    if (!plan || !status) return set_error(FYG_ERR_NULL_PTR, "null argument");
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev != plan->device) cudaSetDevice(plan->device);
+    int word = 0;
+    cudaError_t e = cudaMemcpyAsync(&word, plan->errword.ptr, sizeof(int), cudaMemcpyDeviceToHost,
+                                    (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(plan->errword.ptr, 0, sizeof(int), (cudaStream_t)stream);
+    if (dev != plan->device) cudaSetDevice(dev);
+    if (e != cudaSuccess) return cuda_error(e, "plan status");
+    *status = word;
     return FYG_OK;
 }
 

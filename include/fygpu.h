@@ -61,6 +61,11 @@ extern "C" {
 #define FYG_FLAG_WIDE_TILES 0x40 /* register-resident passes in 512-thread CTAs with twice the
                                   * columns (wider contiguous row segments); chosen per length by
                                   * the autotuner */
+#define FYG_FLAG_TMA_LOADS 0x80  /* every register-resident pass after the first loads its tiles
+                                  * with TMA tensor copies (cp.async.bulk.tensor) into shared
+                                  * memory; by default only 4-column tiles do (measured faster
+                                  * there, slower on wider tiles) */
+#define FYG_FLAG_NO_TMA_LOADS 0x100 /* per-thread loads everywhere (comparisons) */
 
 typedef struct fyg_plan fyg_plan;
 typedef struct fyg_batch fyg_batch;
@@ -122,6 +127,12 @@ int fyg_gpu_strategy(size_t n);
 /* Plan introspection: algorithm length (conv length M for Rader/Bluestein), number of kernel
  * passes per direction, and the GPU strategy. */
 int fyg_plan_info(const fyg_plan* plan, size_t* conv_length, int* passes, int* strategy);
+
+/* Device-side error bits the plan's kernels recorded since the last call (synchronizes the
+ * stream, then clears them): 1 = a stage radix the kernel was not compiled for, 4 = a TMA tile
+ * load that did not complete within its bounded wait.  0 = no error.  Kernels record such
+ * conditions instead of trapping, so the context stays usable. */
+int fyg_plan_status(fyg_plan* plan, void* stream, int* status);
 
 /* Plan whose user buffers hold the batch's transforms `idist` (input) and `odist` (output)
  * elements apart (0 = n, contiguous; otherwise >= n).  The elements between transforms are

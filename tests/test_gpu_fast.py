@@ -125,3 +125,29 @@ def test_wide_tiles(n, batch, inverse):
         ref = O.fft(x[b], inverse=inverse)
         assert O.rel_l2(y[b], ref) <= 2e-6 and O.rel_l2(y[b], ref) <= 4 * np.log2(n) * EPS32
         assert O.rel_l2(y[b], yn[b]) <= 2e-7
+
+
+# TMA tile loads (FYG_FLAG_TMA_LOADS): the same values arrive by tensor copies, so the outputs are
+# identical to the per-thread-load path, and no bounded wait expired
+@pytest.mark.parametrize("n,batch", [(1 << 16, 8), (1 << 20, 3), (1 << 21, 2), (65537, 3), (131074, 2),
+                                     (999983, 2), (1 << 24, 1)])
+@pytest.mark.parametrize("inverse", [False, True])
+def test_tma_loads_match_per_thread_loads(n, batch, inverse):
+    x = fg.fill_random(21, n * batch, np.complex64, "normal")
+    t = torch.from_numpy(x).cuda()
+    pt = fg.FFT1D_C2C_invoker(n, "complex64", batch, flags=fg.FYG_FLAG_TMA_LOADS)
+    pn = fg.FFT1D_C2C_invoker(n, "complex64", batch, flags=fg.FYG_FLAG_NO_TMA_LOADS)
+    yt, yn = torch.empty_like(t), torch.empty_like(t)
+    pt.dispatch(inverse, t, yt)
+    pn.dispatch(inverse, t, yn)
+    torch.cuda.synchronize()
+    assert pt.status() == 0
+    assert torch.equal(yt, yn)
+    # the default plan (TMA on 4-column tiles only) computes the same values too
+    pd = fg.FFT1D_C2C_invoker(n, "complex64", batch)
+    yd = torch.empty_like(t)
+    pd.dispatch(inverse, t, yd)
+    torch.cuda.synchronize()
+    assert pd.status() == 0 and torch.equal(yd, yn)
+    ref = O.fft(x.reshape(batch, n)[batch - 1], inverse=inverse)
+    assert O.rel_l2(yt.view(batch, n)[batch - 1].cpu().numpy(), ref) <= 2e-6
