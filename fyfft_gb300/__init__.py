@@ -31,6 +31,7 @@ FYG_FORWARD, FYG_INVERSE = 1, -1
 FYG_FLAG_CONV_FP64, FYG_FLAG_CONV_FP32, FYG_FLAG_NO_L2_CHUNK = 1, 2, 4
 FYG_FLAG_SMALL_TILES, FYG_FLAG_AUTOTUNED, FYG_FLAG_GENERIC_KERNELS = 8, 16, 32
 FYG_FLAG_WIDE_TILES, FYG_FLAG_TMA_LOADS, FYG_FLAG_NO_TMA_LOADS = 64, 128, 256
+FYG_FLAG_BATCH_BRANCHES = 512
 
 # every symbol include/fygpu.h declares
 EXPORTED_SYMBOLS = (
@@ -43,7 +44,7 @@ EXPORTED_SYMBOLS = (
     "fyg_fill_random_device", "fyg_version", "fyg_plan_cache_stats", "fyg_plan_cache_clear",
     "fyg_partition", "fyg_multi_create", "fyg_multi_shards", "fyg_multi_execute", "fyg_multi_execute_device",
     "fyg_multi_synchronize", "fyg_multi_destroy", "fyg_fill_random_at", "fyg_fill_random_device_at",
-    "fyg_plan_status",
+    "fyg_plan_status", "fyg_execute_async", "fyg_batch_create_ex",
 )
 
 
@@ -79,6 +80,7 @@ def lib() -> ctypes.CDLL:
         L.fyg_autotune.argtypes = [sz, i, sz, ctypes.c_char_p, ctypes.POINTER(d)]
         L.fyg_plan_destroy.argtypes = [vp]
         L.fyg_execute.argtypes = [vp, vp, vp, i, vp]
+        L.fyg_execute_async.argtypes = [vp, vp, vp, i, vp]
         L.fyg_execute_adjoint.argtypes = [vp, vp, vp, d, vp]
         L.fyg_strategy.argtypes = [sz]
         L.fyg_gpu_strategy.argtypes = [sz]
@@ -89,6 +91,7 @@ def lib() -> ctypes.CDLL:
         L.fyg_plan_profile_read.argtypes = [vp, ctypes.POINTER(d), ctypes.POINTER(ctypes.c_int64),
                                             ctypes.POINTER(ctypes.c_int64), i, ctypes.POINTER(i)]
         L.fyg_batch_create.argtypes = [ctypes.POINTER(sz), sz, i, i, ctypes.POINTER(vp)]
+        L.fyg_batch_create_ex.argtypes = [ctypes.POINTER(sz), sz, i, i, i, sz, i, i, ctypes.POINTER(vp)]
         L.fyg_batch_autotune.argtypes = [ctypes.POINTER(sz), sz, i, ctypes.c_char_p, ctypes.POINTER(d)]
         L.fyg_batch_destroy.argtypes = [vp]
         L.fyg_batch_execute.argtypes = [vp, vp, vp, vp, i, vp]
@@ -257,11 +260,13 @@ class FFT1D_C2C_invoker:
             raise ValueError(f"buffers hold {nx}/{ny} complex elements, plan needs {need_x}/{need_y}")
         return px, py
 
-    def dispatch(self, invert: bool, input, output, stream=None) -> None:
-        """foye_FFT.hpp:128-151: dispatch<invert>(input, output)."""
+    def dispatch(self, invert: bool, input, output, stream=None, blocking: bool = True) -> None:
+        """foye_FFT.hpp:128-151: dispatch<invert>(input, output).  blocking=False with host
+        buffers returns after enqueueing (fyg_execute_async): synchronize `stream` before
+        reading `output`."""
         px, py = self._io(input, output)
-        check(lib().fyg_execute(self._h, px, py, FYG_INVERSE if invert else FYG_FORWARD,
-                                _stream_handle(stream)))
+        fn = lib().fyg_execute if blocking else lib().fyg_execute_async
+        check(fn(self._h, px, py, FYG_INVERSE if invert else FYG_FORWARD, _stream_handle(stream)))
 
     def forward(self, input, output, stream=None) -> None:
         self.dispatch(False, input, output, stream)
@@ -326,12 +331,19 @@ class FFT1D_C2C_invoker:
 class UnevenBatch:
     """Many transforms of different lengths packed back to back, run by one persistent kernel."""
 
-    def __init__(self, lengths, dtype="complex64", flags: int = 0):
+    def __init__(self, lengths, dtype="complex64", flags: int = 0, form=None, split: int = 0, radix_cap: int = 0,
+                 single_tile_kb: int = 0):
+        """form None: by flags (the tuner's choice with FYG_FLAG_AUTOTUNED); 0 persistent kernel,
+        1 graph branches, 2 persistent up to `split` and branches above (fyg_batch_create_ex)."""
         self.lengths = [int(n) for n in lengths]
         self.dtype_code = FYG_C32 if str(dtype).endswith("complex64") else FYG_C64
         arr = (ctypes.c_size_t * len(self.lengths))(*self.lengths)
         h = ctypes.c_void_p()
-        check(lib().fyg_batch_create(arr, len(self.lengths), self.dtype_code, flags, ctypes.byref(h)))
+        if form is None:
+            check(lib().fyg_batch_create(arr, len(self.lengths), self.dtype_code, flags, ctypes.byref(h)))
+        else:
+            check(lib().fyg_batch_create_ex(arr, len(self.lengths), self.dtype_code, flags, int(form), int(split),
+                                            int(radix_cap), int(single_tile_kb), ctypes.byref(h)))
         self._h = h
         self.offsets = np.concatenate([[0], np.cumsum(self.lengths)[:-1]]).astype(np.int64)
         self.total = int(sum(self.lengths))

@@ -157,6 +157,15 @@ struct fyg_batch {
     std::map<GraphKey, cudaGraphExec_t> graphs;
     cudaStream_t cap_stream = nullptr;
     int last_grid = 0;
+    // branch form (FYG_FLAG_BATCH_BRANCHES): one regular plan per distinct length (batch =
+    // multiplicity, register-resident kernels where they apply) whose passes address the packed
+    // buffers through the offsets table; the plans run as parallel chains of one captured graph
+    bool branches = false;
+    std::map<size_t, fyg_plan*> branch_plans;
+    std::map<size_t, int> branch_id0;          // first entry of the length's members in d_branch_ids
+    DevBuf d_branch_ids;
+    std::vector<cudaStream_t> branch_streams;
+    std::vector<cudaEvent_t> branch_events;    // fork event, then one join event per stream
 
     int* done_ptr() { return reinterpret_cast<int*>(d_state.ptr); }
     int* head_ptr() { return done_ptr() + n_descs; }
@@ -166,6 +175,9 @@ struct fyg_batch {
     ~fyg_batch() {
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
         if (cap_stream) cudaStreamDestroy(cap_stream);
+        for (cudaStream_t s : branch_streams) cudaStreamDestroy(s);
+        for (cudaEvent_t e : branch_events) cudaEventDestroy(e);
+        for (auto& kv : branch_plans) fyg_plan_destroy(kv.second);
         for (auto& kv : group_plans) fyg_plan_destroy(kv.second);
         for (auto& kv : single_plans) fyg_plan_destroy(kv.second);
     }
@@ -297,6 +309,9 @@ std::string batch_key(const size_t* lengths, size_t count, int dtype) {
     return buf;
 }
 
+// The batch autotuner's candidate, used by fyg_batch_create in place of a cache entry while set.
+thread_local const TuneChoice* g_candidate = nullptr;
+
 // Sets the group-plan options for this thread while alive.
 struct BatchOptions {
     BatchOptions(int radix_cap, int single_kb) { set_batch_tile_options(radix_cap, (size_t)single_kb << 10); }
@@ -305,7 +320,113 @@ struct BatchOptions {
 
 }  // namespace
 
+namespace {
+
+// The branch form: every distinct length's plan is a chain of kernels on one of up to 32 streams
+// forked from the capture stream (lengths with the most work first, each to the least loaded
+// stream), joined back, captured once per (direction, buffers, offsets) and replayed.
+int capture_branches(fyg_batch* b, const void* in, void* out, const int64_t* offs, int direction,
+                     cudaStream_t cap) {
+    const size_t eb = b->dtype == FYG_C32 ? 8 : 16;
+    const int nb = (int)std::min<size_t>(32, b->branch_plans.size());
+    while ((int)b->branch_streams.size() < nb) {
+        cudaStream_t s;
+        cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return cuda_error(e, "branch stream");
+        b->branch_streams.push_back(s);
+    }
+    while ((int)b->branch_events.size() < nb + 1) {
+        cudaEvent_t ev;
+        cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_error(e, "branch event");
+        b->branch_events.push_back(ev);
+    }
+    cudaError_t e = cudaEventRecord(b->branch_events[0], cap);
+    for (int k = 0; k < nb && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(b->branch_streams[k], b->branch_events[0], 0);
+    if (e != cudaSuccess) return cuda_error(e, "branch fork");
+    std::vector<std::pair<double, size_t>> work;
+    for (auto& kv : b->members) {
+        if (!b->branch_plans.count(kv.first)) continue;   // in the persistent kernel
+        const double n = (double)kv.first;
+        work.push_back({n * std::max(1.0, std::log2(n)) * (double)kv.second.size(), kv.first});
+    }
+    std::sort(work.rbegin(), work.rend());
+    std::vector<double> load(nb, 0.0);
+    const int* ids = reinterpret_cast<const int*>(b->d_branch_ids.ptr);
+    for (auto& w : work) {
+        const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[k] += w.first;
+        const cudaStream_t s = b->branch_streams[k];
+        fyg_plan* pl = b->branch_plans[w.second];
+        if (pl->strategy == GS_COPY) {
+            // length 1: the identity, one element per member (host offsets)
+            for (int m : b->members[w.second]) {
+                const int64_t o = b->offsets[m];
+                e = cudaMemcpyAsync((char*)out + o * eb, (const char*)in + o * eb, eb, cudaMemcpyDeviceToDevice, s);
+                if (e != cudaSuccess) return cuda_error(e, "length-1 copy");
+            }
+            continue;
+        }
+        const int rc = run_plan_offsets(pl, in, out, offs, ids + b->branch_id0[w.second], direction, s);
+        if (rc) return rc;
+    }
+    // the persistent kernel (shorter lengths) on the capture stream, alongside the branches
+    if (b->persistent) {
+        const int rc = launch_persistent(b, in, out, offs == reinterpret_cast<const int64_t*>(b->d_offsets.ptr) ? nullptr : offs,
+                                         direction, cap);
+        if (rc) return rc;
+    }
+    for (int k = 0; k < nb && e == cudaSuccess; ++k) {
+        e = cudaEventRecord(b->branch_events[k + 1], b->branch_streams[k]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(cap, b->branch_events[k + 1], 0);
+    }
+    return e == cudaSuccess ? FYG_OK : cuda_error(e, "branch join");
+}
+
+}  // namespace
+
+static int execute_branches(fyg_batch* b, const void* in, void* out, const int64_t* offsets_dev, int direction,
+                            cudaStream_t st) {
+    const int64_t* offs = offsets_dev ? offsets_dev : reinterpret_cast<const int64_t*>(b->d_offsets.ptr);
+    fyg_batch::GraphKey key{direction, in, out, offsets_dev};
+    auto it = b->graphs.find(key);
+    if (it == b->graphs.end()) {
+        if (!b->cap_stream) {
+            cudaError_t e = cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking);
+            if (e != cudaSuccess) return cuda_error(e, "capture stream");
+        }
+        cudaError_t e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_error(e, "begin capture");
+        int rc = capture_branches(b, in, out, offs, direction, b->cap_stream);
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(b->cap_stream, &g);
+        if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+        if (e != cudaSuccess) return cuda_error(e, "end capture");
+        cudaGraphExec_t ex = nullptr;
+        e = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_error(e, "graph instantiate");
+        it = b->graphs.emplace(key, ex).first;
+    }
+    const cudaError_t e = cudaGraphLaunch(it->second, st);
+    return e == cudaSuccess ? FYG_OK : cuda_error(e, "graph launch");
+}
+
 extern "C" {
+
+int fyg_batch_create_ex(const size_t* lengths, size_t count, int dtype, int flags, int form, size_t split,
+                        int radix_cap, int single_tile_kb, fyg_batch** out) {
+    if (form < 0 || form > 2) return set_error(FYG_ERR_INVALID_ARG, "form must be 0, 1 or 2");
+    TuneChoice cc;
+    cc.max_pass_radix = (uint64_t)std::max(radix_cap, 0);
+    cc.cols = std::max(single_tile_kb, 0);
+    cc.order = form;
+    cc.conv_length = (uint64_t)split;
+    g_candidate = &cc;
+    const int rc = fyg_batch_create(lengths, count, dtype, flags | FYG_FLAG_AUTOTUNED, out);
+    g_candidate = nullptr;
+    return rc;
+}
 
 int fyg_batch_create(const size_t* lengths, size_t count, int dtype, int flags, fyg_batch** out) {
     clear_error();
@@ -313,8 +434,19 @@ int fyg_batch_create(const size_t* lengths, size_t count, int dtype, int flags, 
     *out = nullptr;
     if (dtype != FYG_C32 && dtype != FYG_C64) return set_error(FYG_ERR_INVALID_ARG, "bad dtype");
     TuneChoice tc;
-    if ((flags & FYG_FLAG_AUTOTUNED) && !tune_lookup_key(batch_key(lengths, count, dtype), &tc)) tc = TuneChoice();
-    flags &= ~FYG_FLAG_AUTOTUNED;
+    if (flags & FYG_FLAG_AUTOTUNED) {
+        if (g_candidate) tc = *g_candidate;
+        else if (!tune_lookup_key(batch_key(lengths, count, dtype), &tc)) tc = TuneChoice();
+    }
+    // lengths above `split` run in the branch form, the others in the persistent kernel:
+    // SIZE_MAX by default, 0 with FYG_FLAG_BATCH_BRANCHES, else the tuner's choice (order 1:
+    // all branches, order 2: the split stored in conv_length); FP64 batches have no persistent
+    // kernel and run in the branch form
+    size_t split = SIZE_MAX;
+    if ((flags & FYG_FLAG_AUTOTUNED) && tc.order == 1) split = 0;
+    if ((flags & FYG_FLAG_AUTOTUNED) && tc.order == 2) split = (size_t)tc.conv_length;
+    if ((flags & FYG_FLAG_BATCH_BRANCHES) || dtype != FYG_C32) split = 0;
+    flags &= ~(FYG_FLAG_AUTOTUNED | FYG_FLAG_BATCH_BRANCHES);
     BatchOptions opts((int)tc.max_pass_radix, tc.cols);
     auto b = std::make_unique<fyg_batch>();
     b->dtype = dtype;
@@ -328,17 +460,41 @@ int fyg_batch_create(const size_t* lengths, size_t count, int dtype, int flags, 
         off += (int64_t)lengths[i];
     }
     for (auto& kv : b->members) {
-        fyg_plan* p = nullptr;
-        int rc = fyg_plan_create(kv.first, dtype, kv.second.size(),
-                                 flags | FYG_FLAG_NO_L2_CHUNK | FYG_FLAG_SMALL_TILES, &p);
-        if (rc) return rc;
-        b->group_plans[kv.first] = p;
+        if (kv.first <= split) {
+            fyg_plan* p = nullptr;
+            int rc = fyg_plan_create(kv.first, dtype, kv.second.size(),
+                                     flags | FYG_FLAG_NO_L2_CHUNK | FYG_FLAG_SMALL_TILES, &p);
+            if (rc) return rc;
+            b->group_plans[kv.first] = p;
+        }
     }
-    if (dtype == FYG_C32 && count > 0) {
+    if (!b->group_plans.empty()) {
         int rc = build_persistent(b.get());
         if (rc == FYG_OK) b->persistent = true;
         else if (rc != FYG_ERR_UNSUPPORTED) return rc;
         clear_error();
+        if (!b->persistent) {   // no persistent kernel for these plans: they join the branch form
+            for (auto& kv : b->group_plans) fyg_plan_destroy(kv.second);
+            b->group_plans.clear();
+            split = 0;
+        }
+    }
+    std::vector<int> ids;
+    for (auto& kv : b->members) {
+        if (kv.first <= split) continue;
+        fyg_plan* p = nullptr;
+        int rc = fyg_plan_create(kv.first, dtype, kv.second.size(), flags | FYG_FLAG_NO_L2_CHUNK, &p);
+        if (rc) return rc;
+        b->branch_plans[kv.first] = p;
+        b->branch_id0[kv.first] = (int)ids.size();
+        ids.insert(ids.end(), kv.second.begin(), kv.second.end());
+    }
+    if (!b->branch_plans.empty()) {
+        b->branches = true;
+        int rc = b->d_branch_ids.upload(ids.data(), ids.size() * sizeof(int));
+        if (!rc && !b->persistent)
+            rc = b->d_offsets.upload(b->offsets.data(), std::max<size_t>(b->offsets.size(), 1) * sizeof(int64_t));
+        if (rc) return rc;
     }
     *out = b.release();
     return FYG_OK;
@@ -378,11 +534,8 @@ int fyg_batch_execute(fyg_batch* b, const void* in, void* out, const int64_t* of
         return set_error(FYG_ERR_INVALID_ARG, "direction must be FYG_FORWARD or FYG_INVERSE");
     if (b->lengths.empty()) return FYG_OK;
     const cudaStream_t st = (cudaStream_t)stream;
-    if (!b->persistent) {
-        // FP64 batches: one launch sequence per group of equal lengths
-        if (offsets_dev) return set_error(FYG_ERR_UNSUPPORTED, "custom offsets need an FP32 batch");
-        return fyg_batch_execute_plain(b, in, out, direction, stream);
-    }
+    if (b->branches) return execute_branches(b, in, out, offsets_dev, direction, st);
+    if (!b->persistent) return set_error(FYG_ERR_UNSUPPORTED, "batch has no execution form");
     fyg_batch::GraphKey key{direction, in, out, offsets_dev};
     auto it = b->graphs.find(key);
     if (it == b->graphs.end()) {
@@ -411,6 +564,16 @@ int fyg_batch_execute(fyg_batch* b, const void* in, void* out, const int64_t* of
 int fyg_batch_status(fyg_batch* b, void* stream) {
     clear_error();
     if (!b) return set_error(FYG_ERR_NULL_PTR, "null batch");
+    if (b->branches) {
+        // the device error bits of every branch length's plan
+        for (auto& kv : b->branch_plans) {
+            int st = 0;
+            const int rc = fyg_plan_status(kv.second, stream, &st);
+            if (rc) return rc;
+            if (st) return set_error(FYG_ERR_CUDA, "kernel error bits " + std::to_string(st) + " (length " +
+                                                       std::to_string(kv.first) + ")");
+        }
+    }
     if (!b->persistent) return FYG_OK;
     cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_error(e, "stream synchronize");
@@ -463,7 +626,10 @@ extern "C" int fyg_batch_autotune(const size_t* lengths, size_t count, int dtype
     if (!rc) rc = fyg_fill_random_device(11, 1, dtype, total, in.ptr, nullptr);
     if (rc) return rc;
     const bool verbose = std::getenv("FYG_AUTOTUNE_VERBOSE") != nullptr;
-    const int cand[][2] = {{16, 100}, {32, 100}, {16, 48}, {32, 160}};
+    // {stage radix cap, single-pass tile KB, form, split}: form 0 persistent kernel, 1 branches,
+    // 2 lengths up to `split` in the persistent kernel and the longer ones in branches
+    const int cand[][4] = {{16, 100, 0, 0}, {32, 100, 0, 0}, {16, 48, 0, 0}, {32, 160, 0, 0}, {0, 0, 1, 0},
+                           {16, 100, 2, 4096}, {16, 100, 2, 16384}, {32, 100, 2, 4096}};
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -471,12 +637,12 @@ extern "C" int fyg_batch_autotune(const size_t* lengths, size_t count, int dtype
     bool have = false;
     for (const auto& c : cand) {
         fyg_batch* b = nullptr;
-        {
-            BatchOptions opts(c[0], c[1]);
-            if (fyg_batch_create(lengths, count, dtype, 0, &b) != FYG_OK) continue;
-        }
+        const bool br = c[2] == 1;
+        if (fyg_batch_create_ex(lengths, count, dtype, 0, c[2], (size_t)c[3], c[0], c[1], &b) != FYG_OK) continue;
         double t = 1e30;
-        bool ok = b->persistent && fyg_batch_execute(b, in.ptr, out.ptr, nullptr, FYG_FORWARD, nullptr) == FYG_OK;
+        (void)br;
+        bool ok = (b->persistent || b->branches) &&
+                  fyg_batch_execute(b, in.ptr, out.ptr, nullptr, FYG_FORWARD, nullptr) == FYG_OK;
         for (int rep = 0; rep < 3 && ok; ++rep) {
             cudaEventRecord(e0, nullptr);
             ok = fyg_batch_execute(b, in.ptr, out.ptr, nullptr, FYG_FORWARD, nullptr) == FYG_OK;
@@ -488,12 +654,14 @@ extern "C" int fyg_batch_autotune(const size_t* lengths, size_t count, int dtype
         }
         fyg_batch_destroy(b);
         if (verbose)
-            std::fprintf(stderr, "fyg_batch_autotune radix_cap=%d single_tile_kb=%d: %s %.4f ms\n", c[0], c[1],
-                         ok ? "ok" : "failed", ok ? t : 0.0);
+            std::fprintf(stderr, "fyg_batch_autotune form=%d split=%d radix_cap=%d single_tile_kb=%d: %s %.4f ms\n",
+                         c[2], c[3], c[0], c[1], ok ? "ok" : "failed", ok ? t : 0.0);
         if (ok && (!have || t < best.ms)) {
             best = TuneChoice();
             best.max_pass_radix = (uint64_t)c[0];
             best.cols = c[1];
+            best.order = c[2];
+            best.conv_length = (uint64_t)c[3];
             best.ms = t;
             have = true;
         }

@@ -58,6 +58,9 @@ int tune_store_key(const std::string& key, const TuneChoice& choice, const char*
 void set_batch_tile_options(int radix_cap, size_t single_cap_bytes);
 int plan_create_opts(size_t n, int dtype, size_t batch, int flags, uint64_t max_pass_radix, uint64_t conv_length,
                      int cols, int order, int threads, fyg_plan** out);
+// A plan's whole batch with its user transforms at element offsets offs[ids[b]] (device tables).
+int run_plan_offsets(fyg_plan* pl, const void* in, void* out, const int64_t* offs, const int* ids, int direction,
+                     cudaStream_t st);
 // Layout of the user buffers of plans created next on this thread (0 = contiguous).
 void set_plan_layout(size_t idist, size_t odist);
 void host_two_level(uint64_t L, int cb, std::vector<unsigned char>& hi, std::vector<unsigned char>& lo, int* shift);
@@ -128,6 +131,9 @@ struct fyg_plan {
     // copies of one batch chunk overlap the kernels of the previous one
     cudaStream_t s_h2d = nullptr, s_d2h = nullptr;
     std::vector<cudaEvent_t> stage_ev;
+    // recorded when this plan's last call finished reading stage_in (its kernels) and stage_out
+    // (its copy-out): the next call's copy-in and kernels wait on them
+    cudaEvent_t ev_in_free = nullptr, ev_out_free = nullptr;
     // instrumentation: event pairs per launch, accumulated per forward pass
     bool profile = false;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;

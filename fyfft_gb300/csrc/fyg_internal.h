@@ -57,6 +57,7 @@ cudaError_t launch_fill_random(uint64_t seed, int dist, int dtype, size_t first,
                                cudaStream_t st);
 
 // Small helper kernels.
+cudaError_t launch_delay(unsigned long long ns, cudaStream_t st);
 cudaError_t launch_convert_d2f(const double2* in, float2* out, size_t n, cudaStream_t st);
 
 }  // namespace fyg

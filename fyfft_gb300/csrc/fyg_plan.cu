@@ -970,8 +970,11 @@ static int make_plan(fyg_plan* pl) {
 // ------------------------------------------------------------------------------------------
 
 // Runs the pipeline over transforms [b_begin, b_end) of the batch (in/out are the batch bases).
+// offs / ids (uneven batches): transform b of the user buffers starts at element offs[ids[b]]
+// instead of b * idist (whole batch in one chunk).
 static int run_pipeline(fyg_plan* pl, const std::vector<PassDesc>& pipe, const void* in, void* out,
-                        double final_scale_mul, cudaStream_t st, size_t b_begin = 0, size_t b_end = SIZE_MAX) {
+                        double final_scale_mul, cudaStream_t st, size_t b_begin = 0, size_t b_end = SIZE_MAX,
+                        const int64_t* offs = nullptr, const int* ids = nullptr) {
     const int io_cb = pl->dtype == FYG_C32 ? 8 : 16;
     b_end = std::min(b_end, pl->batch);
     for (size_t c0 = b_begin; c0 < b_end; c0 += pl->chunk) {
@@ -989,6 +992,10 @@ static int run_pipeline(fyg_plan* pl, const std::vector<PassDesc>& pipe, const v
             };
             p.in = resolve(d.in_role);
             p.out = resolve(d.out_role);
+            if (offs) {
+                if (d.in_role == ROLE_IN) { p.in = in; p.in_offsets = offs; p.ids = ids; }
+                if (d.out_role == ROLE_OUT) { p.out = out; p.out_offsets = offs; p.ids = ids; }
+            }
             p.ncols = (int64_t)nb * p.Rr;
             p.x0buf = pl->x0buf.ptr;
             p.dcbuf = pl->dcbuf.ptr;
@@ -1066,8 +1073,24 @@ static int ensure_staging(fyg_plan* pl) {
     return FYG_OK;
 }
 
+// async: return after enqueueing; the caller's stream reaches completion when the output is in
+// host memory, and the host input is read by the copy stream without waiting for earlier work
+// on the caller's stream (the caller has it ready), so consecutive calls of different plans
+// pipeline their copies and kernels.  Otherwise the copy-in waits for earlier work on the
+// caller's stream and the call returns when the output is in host memory.
+// Asynchronous calls of one host thread on one device keep their copies in call order: each
+// call's first copy-in waits for the previous call's last copy-in, and likewise for copy-outs, so
+// the copy engines serve the transforms first in, first out (concurrent copy streams of many
+// plans were measured to slow the first transforms and with them the whole pipeline).
+namespace {
+struct CopyChain {
+    cudaEvent_t h2d = nullptr, d2h = nullptr;
+};
+thread_local std::map<int, CopyChain> t_chain;
+}  // namespace
+
 static int execute_host_overlapped(fyg_plan* pl, const void* in, void* out, bool inverse, double scale_mul,
-                                   cudaStream_t st) {
+                                   cudaStream_t st, bool async) {
     int rc = ensure_staging(pl);
     if (rc) return rc;
     // about 8 chunks, whole transforms, at least one L2 chunk of the plan each
@@ -1085,11 +1108,33 @@ static int execute_host_overlapped(fyg_plan* pl, const void* in, void* out, bool
         if (e != cudaSuccess) return cuda_error(e, "staging events");
         pl->stage_ev.push_back(ev);
     }
+    if (!pl->ev_in_free) {
+        cudaError_t e = cudaEventCreateWithFlags(&pl->ev_in_free, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pl->ev_out_free, cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_error(e, "staging events");
+    }
     cudaEvent_t start = pl->stage_ev[2 * nch];
     auto chk = [&](cudaError_t e, const char* what) { return e == cudaSuccess ? FYG_OK : cuda_error(e, what); };
-    // earlier work on the caller's stream may still read the staging buffers
-    rc = chk(cudaEventRecord(start, st), "event");
-    if (!rc) rc = chk(cudaStreamWaitEvent(pl->s_h2d, start, 0), "wait");
+    // the staging buffers of this plan: its previous call's kernels may still read stage_in and
+    // its previous copy-out may still read stage_out (waits on never-recorded events are no-ops)
+    rc = chk(cudaStreamWaitEvent(pl->s_h2d, pl->ev_in_free, 0), "wait");
+    if (!rc) rc = chk(cudaStreamWaitEvent(st, pl->ev_out_free, 0), "wait");
+    if (!async && !rc) {
+        // ordered after earlier work on the caller's stream
+        rc = chk(cudaEventRecord(start, st), "event");
+        if (!rc) rc = chk(cudaStreamWaitEvent(pl->s_h2d, start, 0), "wait");
+    }
+    CopyChain* chain = nullptr;
+    if (async && !rc) {
+        chain = &t_chain[pl->device];
+        if (!chain->h2d) {
+            cudaError_t e = cudaEventCreateWithFlags(&chain->h2d, cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&chain->d2h, cudaEventDisableTiming);
+            if (e != cudaSuccess) return cuda_error(e, "copy chain events");
+        }
+        rc = chk(cudaStreamWaitEvent(pl->s_h2d, chain->h2d, 0), "wait");
+        if (!rc) rc = chk(cudaStreamWaitEvent(pl->s_d2h, chain->d2h, 0), "wait");
+    }
     const char* hin = static_cast<const char*>(in);
     char* hout = static_cast<char*>(out);
     char* sin = static_cast<char*>(pl->stage_in.ptr);
@@ -1107,7 +1152,14 @@ static int execute_host_overlapped(fyg_plan* pl, const void* in, void* out, bool
             rc = chk(copy_rows(hout, sout, pl, pl->odist, b0, nb, cudaMemcpyDeviceToHost, pl->s_d2h),
                      "device->host staging");
     }
-    // always drain both copy streams before returning (the host buffers are the caller's)
+    if (!rc) rc = chk(cudaEventRecord(pl->ev_in_free, st), "event");
+    if (!rc) rc = chk(cudaEventRecord(pl->ev_out_free, pl->s_d2h), "event");
+    if (chain && !rc) {
+        rc = chk(cudaEventRecord(chain->h2d, pl->s_h2d), "event");
+        if (!rc) rc = chk(cudaEventRecord(chain->d2h, pl->s_d2h), "event");
+    }
+    if (async && !rc) return chk(cudaStreamWaitEvent(st, pl->ev_out_free, 0), "wait");
+    // drain both copy streams before returning (the host buffers are the caller's)
     const cudaError_t e1 = cudaStreamSynchronize(pl->s_h2d);
     const cudaError_t e2 = cudaStreamSynchronize(pl->s_d2h);
     if (!rc) rc = chk(e1, "stream synchronize");
@@ -1115,7 +1167,8 @@ static int execute_host_overlapped(fyg_plan* pl, const void* in, void* out, bool
     return rc;
 }
 
-static int execute_dir(fyg_plan* pl, const void* in, void* out, bool inverse, double scale_mul, cudaStream_t st) {
+static int execute_dir(fyg_plan* pl, const void* in, void* out, bool inverse, double scale_mul, cudaStream_t st,
+                       bool async = false) {
     if (!pl) return set_error(FYG_ERR_NULL_PTR, "null plan");
     if (!in || !out) return set_error(FYG_ERR_NULL_PTR, "null buffer");
     const int io_cb = pl->dtype == FYG_C32 ? 8 : 16;
@@ -1140,7 +1193,7 @@ static int execute_dir(fyg_plan* pl, const void* in, void* out, bool inverse, do
         return set_error(FYG_ERR_INVALID_ARG, "buffers on another device than the plan's");
     const bool din = kin > 0, dout = kout > 0;
     if (!din && !dout && pl->strategy != GS_COPY && pl->batch >= 2 && bytes >= (8u << 20))
-        return execute_host_overlapped(pl, in, out, inverse, scale_mul, st);
+        return execute_host_overlapped(pl, in, out, inverse, scale_mul, st, async);
     const void* din_p = in;
     void* dout_p = out;
     int rc = FYG_OK;
@@ -1165,7 +1218,7 @@ static int execute_dir(fyg_plan* pl, const void* in, void* out, bool inverse, do
         cudaError_t e = copy_rows(out, dout_p, pl, pl->odist, 0, pl->batch, cudaMemcpyDeviceToHost, st);
         if (e != cudaSuccess) return cuda_error(e, "device->host staging");
     }
-    if (!din || !dout) {
+    if ((!din || !dout) && !async) {
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return cuda_error(e, "stream synchronize");
     }
@@ -1214,6 +1267,12 @@ static int gpu_fft_f64(size_t n, const std::vector<double2>& h, std::vector<doub
 using namespace fyg;
 
 fyg_plan::~fyg_plan() {
+    // pending asynchronous host executions still use the staging buffers and copy streams
+    if (s_h2d) cudaStreamSynchronize(s_h2d);
+    if (s_d2h) cudaStreamSynchronize(s_d2h);
+    if (ev_in_free) cudaEventSynchronize(ev_in_free);
+    if (ev_in_free) cudaEventDestroy(ev_in_free);
+    if (ev_out_free) cudaEventDestroy(ev_out_free);
     for (cudaEvent_t e : prof_pool) cudaEventDestroy(e);
     for (cudaEvent_t e : stage_ev) cudaEventDestroy(e);
     if (s_h2d) cudaStreamDestroy(s_h2d);
@@ -1221,6 +1280,20 @@ fyg_plan::~fyg_plan() {
 }
 
 namespace fyg {
+// Enqueues a plan's whole batch on `st` with its user transforms at packed offsets (device
+// tables offs[ids[b]]); used by the branch form of uneven batches.
+int run_plan_offsets(fyg_plan* pl, const void* in, void* out, const int64_t* offs, const int* ids, int direction,
+                     cudaStream_t st) {
+    if (pl->chunk != pl->batch) return set_error(FYG_ERR_UNSUPPORTED, "offset execution needs one chunk");
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev != pl->device) cudaSetDevice(pl->device);
+    const int rc = run_pipeline(pl, direction == FYG_INVERSE ? pl->inv : pl->fwd, in, out, 1.0, st, 0, SIZE_MAX,
+                                offs, ids);
+    if (dev != pl->device) cudaSetDevice(dev);
+    return rc;
+}
+
 void set_plan_layout(size_t idist, size_t odist) {
     t_idist = idist;
     t_odist = odist;
@@ -1391,6 +1464,13 @@ int fyg_execute(fyg_plan* plan, const void* in, void* out, int direction, void* 
     if (direction != FYG_FORWARD && direction != FYG_INVERSE)
         return set_error(FYG_ERR_INVALID_ARG, "direction must be FYG_FORWARD or FYG_INVERSE");
     return execute_dir(plan, in, out, direction == FYG_INVERSE, 1.0, (cudaStream_t)stream);
+}
+
+int fyg_execute_async(fyg_plan* plan, const void* in, void* out, int direction, void* stream) {
+    clear_error();
+    if (direction != FYG_FORWARD && direction != FYG_INVERSE)
+        return set_error(FYG_ERR_INVALID_ARG, "direction must be FYG_FORWARD or FYG_INVERSE");
+    return execute_dir(plan, in, out, direction == FYG_INVERSE, 1.0, (cudaStream_t)stream, true);
 }
 
 int fyg_execute_adjoint(fyg_plan* plan, const void* g, void* out, double scale, void* stream) {

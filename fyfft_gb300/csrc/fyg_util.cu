@@ -134,6 +134,23 @@ void fill_random_host(uint64_t seed, int dist, int dtype, size_t first, size_t n
     for (auto& x : th) x.join();
 }
 
+// A single thread that waits `ns` nanoseconds of %globaltimer (bounded by construction): queued
+// ahead of timed launches so that the host has enqueued all of them before the first starts,
+// and the events around them measure device time rather than host launch latency.
+__global__ void k_delay(unsigned long long ns) {
+    unsigned long long t0, t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    do {
+        __nanosleep(1000);
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    } while (t - t0 < ns);
+}
+
+cudaError_t launch_delay(unsigned long long ns, cudaStream_t st) {
+    k_delay<<<1, 1, 0, st>>>(ns);
+    return cudaGetLastError();
+}
+
 __global__ void k_convert_d2f(const double2* in, float2* out, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         out[i] = make_float2((float)in[i].x, (float)in[i].y);

@@ -66,6 +66,10 @@ extern "C" {
                                   * memory; by default only 4-column tiles do (measured faster
                                   * there, slower on wider tiles) */
 #define FYG_FLAG_NO_TMA_LOADS 0x100 /* per-thread loads everywhere (comparisons) */
+#define FYG_FLAG_BATCH_BRANCHES 0x200 /* uneven batches: one plan per distinct length (register-
+                                       * resident kernels where they apply) as parallel chains of
+                                       * one CUDA graph instead of the persistent kernel; the batch
+                                       * autotuner measures both forms */
 
 typedef struct fyg_plan fyg_plan;
 typedef struct fyg_batch fyg_batch;
@@ -111,6 +115,15 @@ int fyg_plan_cache_clear(void);
  * Replaces fy::fft::FFT1D_C2C_invoker::dispatch<bool invert>(const float*, float*)
  * (foye_FFT.hpp:128-151); the reference runs one transform per call. */
 int fyg_execute(fyg_plan* plan, const void* in, void* out, int direction, void* stream);
+
+/* As fyg_execute, but host buffers do not block: the call enqueues the staged copies and kernels
+ * and returns; the output is in host memory once `stream` has completed (synchronize it before
+ * reading `out` or reusing `in`).  The host input is read without waiting for earlier work on
+ * `stream`, so it must be ready at the call; pinned host memory makes the copies asynchronous.
+ * Consecutive calls of different plans then overlap one plan's copies with another's kernels.
+ * Device buffers: identical to fyg_execute.  No counterpart in the reference (its dispatch is
+ * synchronous). */
+int fyg_execute_async(fyg_plan* plan, const void* in, void* out, int direction, void* stream);
 
 /* Adjoint (conjugate transpose) of the forward transform, times `scale`:
  * out = scale * F^H g = scale * N * dispatch<true>(g).  No counterpart in the reference; its
@@ -170,6 +183,15 @@ int fyg_batch_create(const size_t* lengths, size_t count, int dtype, int flags, 
  * type and a hash of the lengths.  fyg_batch_create with FYG_FLAG_AUTOTUNED uses it.  FYG_C32
  * only.  *best_ms (optional) receives the winner's milliseconds per forward execution. */
 int fyg_batch_autotune(const size_t* lengths, size_t count, int dtype, const char* cache_path, double* best_ms);
+
+/* fyg_batch_create with an explicit execution form (what the batch autotuner chooses between):
+ * form 0: one persistent kernel over a device work queue (stage radix cap 16 or 32, single-pass
+ * tiles up to single_tile_kb KB of shared memory; 0 = defaults); form 1: one plan per distinct
+ * length (register-resident kernels where they apply) as parallel chains of one CUDA graph;
+ * form 2: lengths up to `split` in the persistent kernel, longer ones as graph chains, both in
+ * one graph.  FP64 batches always run form 1. */
+int fyg_batch_create_ex(const size_t* lengths, size_t count, int dtype, int flags, int form, size_t split,
+                        int radix_cap, int single_tile_kb, fyg_batch** out);
 int fyg_batch_destroy(fyg_batch* batch);
 
 /* offsets_dev: device array of `count` int64 element offsets (NULL: packed back to back in the

@@ -104,7 +104,13 @@ def test_batch_autotune_caches_a_choice_and_the_tuned_batch_is_exact(tmp_path):
     keys = [k for k in doc["entries"] if k.startswith("batch32:160:")]
     assert len(keys) == 1
     e = doc["entries"][keys[0]]
-    assert e["max_pass_radix"] in (16, 32) and e["cols"] in (48, 100, 160)
+    # form 0: persistent kernel (stage radix cap, single-pass tile KB); 1: branches; 2: both,
+    # split at the length in conv_length
+    assert e["order"] in (0, 1, 2)
+    if e["order"] != 1:
+        assert e["max_pass_radix"] in (16, 32) and e["cols"] in (48, 100, 160)
+    if e["order"] == 2:
+        assert e["conv_length"] in (4096, 16384)
     b = fg.UnevenBatch(lengths, flags=fg.FYG_FLAG_AUTOTUNED)
     x = fg.fill_random(8, sum(lengths), np.complex64, "uniform")
     xd = torch.from_numpy(x).cuda()
@@ -139,3 +145,58 @@ def test_full_mixed_length_configuration_vs_oracle():
     worst = max(range(len(lengths)), key=lambda i: errs[i])
     assert errs[worst] <= 2e-6, (lengths[worst], errs[worst])
     assert all(e <= 4 * np.log2(n) * float(np.finfo(np.float32).eps) for e, n in zip(errs, lengths))
+
+
+@pytest.mark.parametrize("inverse", [False, True])
+def test_branch_form_matches_persistent_form_and_oracle(batch, inverse):
+    """FYG_FLAG_BATCH_BRANCHES: one plan per distinct length as parallel chains of one graph."""
+    lengths, b, x = batch
+    bb = fg.UnevenBatch(lengths, flags=fg.FYG_FLAG_BATCH_BRANCHES)
+    xd = torch.from_numpy(x).cuda()
+    y, yp = torch.empty_like(xd), torch.empty_like(xd)
+    bb.execute(xd, y, invert=inverse)
+    bb.execute(xd, y, invert=inverse)     # graph replay
+    assert bb.status() == 0
+    b.execute(xd, yp, invert=inverse)
+    torch.cuda.synchronize()
+    for n, xi, yi, ypi in zip(lengths, split(x, lengths), split(y.cpu().numpy(), lengths), split(yp.cpu().numpy(), lengths)):
+        assert O.rel_l2(yi, O.fft(xi, inverse=inverse)) <= 2e-6, n
+        assert O.rel_l2(yi, ypi) <= 2e-6, n
+
+
+def test_branch_form_custom_offsets(batch):
+    lengths, _, x = batch
+    bb = fg.UnevenBatch(lengths, flags=fg.FYG_FLAG_BATCH_BRANCHES)
+    offs, o = [0] * len(lengths), 0
+    for i in reversed(range(len(lengths))):
+        offs[i] = o
+        o += lengths[i]
+    xr = np.empty_like(x)
+    for i, xi in enumerate(split(x, lengths)):
+        xr[offs[i]:offs[i] + lengths[i]] = xi
+    xd = torch.from_numpy(xr).cuda()
+    y = torch.empty_like(xd)
+    bb.execute(xd, y, offsets_dev=torch.tensor(offs, dtype=torch.int64, device="cuda"))
+    assert bb.status() == 0
+    yh = y.cpu().numpy()
+    for i, xi in enumerate(split(x, lengths)):
+        assert O.rel_l2(yh[offs[i]:offs[i] + lengths[i]], O.fft(xi)) <= 2e-6
+
+
+@pytest.mark.parametrize("split", [4096, 16384])
+def test_hybrid_form_matches_oracle(split):
+    """Lengths up to `split` in the persistent kernel, longer ones as graph branches, concurrently."""
+    lengths = uneven_lengths(count=200, seed=9)
+    b = fg.UnevenBatch(lengths, form=2, split=split, radix_cap=16, single_tile_kb=100)
+    x = fg.fill_random(10, sum(lengths), np.complex64, "uniform")
+    xd = torch.from_numpy(x).cuda()
+    y = torch.empty_like(xd)
+    for inverse in (False, True):
+        b.execute(xd, y, invert=inverse)
+        assert b.status() == 0
+        torch.cuda.synchronize()
+        for n, xi, yi in zip(lengths, split_(x, lengths), split_(y.cpu().numpy(), lengths)):
+            assert O.rel_l2(yi, O.fft(xi, inverse=inverse)) <= 2e-6, (n, inverse)
+
+
+split_ = split

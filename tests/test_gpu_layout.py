@@ -92,3 +92,25 @@ def test_layout_in_place_needs_equal_distances():
 def test_layout_rejects_short_distances():
     with pytest.raises(fg.FygError):
         fg.FFT1D_C2C_invoker(4096, "complex64", 2, idist=4000)
+
+
+@pytest.mark.parametrize("n,batch", [(1 << 16, 64), (999983, 4), (2520, 8)])
+def test_async_host_execution_pipelines_and_matches(n, batch):
+    """fyg_execute_async on pinned host buffers: two plans enqueued back to back without
+    blocking, then one stream synchronize; outputs equal the blocking path's."""
+    x1 = torch.from_numpy(fg.fill_random(31, n * batch, np.complex64, "normal")).pin_memory()
+    x2 = torch.from_numpy(fg.fill_random(32, n * batch, np.complex64, "normal")).pin_memory()
+    y1, y2 = torch.empty_like(x1).pin_memory(), torch.empty_like(x2).pin_memory()
+    p1 = fg.FFT1D_C2C_invoker(n, "complex64", batch)
+    p2 = fg.FFT1D_C2C_invoker(n, "complex64", batch)
+    s = torch.cuda.current_stream()
+    for _ in range(2):
+        p1.dispatch(False, x1.numpy(), y1.numpy(), s, blocking=False)
+        p2.dispatch(True, x2.numpy(), y2.numpy(), s, blocking=False)
+        p1.dispatch(False, x1.numpy(), y1.numpy(), s, blocking=False)   # same plan again: staging reuse
+    s.synchronize()
+    r1, r2 = np.empty_like(x1.numpy()), np.empty_like(x2.numpy())
+    p1.dispatch(False, x1.numpy(), r1)
+    p2.dispatch(True, x2.numpy(), r2)
+    assert np.array_equal(y1.numpy(), r1) and np.array_equal(y2.numpy(), r2)
+    assert O.rel_l2(r1.reshape(batch, n)[-1], O.fft(x1.numpy().reshape(batch, n)[-1])) <= 2e-6
