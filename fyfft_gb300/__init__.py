@@ -44,7 +44,7 @@ EXPORTED_SYMBOLS = (
     "fyg_fill_random_device", "fyg_version", "fyg_plan_cache_stats", "fyg_plan_cache_clear",
     "fyg_partition", "fyg_multi_create", "fyg_multi_shards", "fyg_multi_execute", "fyg_multi_execute_device",
     "fyg_multi_synchronize", "fyg_multi_destroy", "fyg_fill_random_at", "fyg_fill_random_device_at",
-    "fyg_plan_status", "fyg_execute_async", "fyg_batch_create_ex",
+    "fyg_plan_status", "fyg_execute_async", "fyg_batch_create_ex", "fyg_plan_join", "fyg_device_signature",
 )
 
 
@@ -81,6 +81,8 @@ def lib() -> ctypes.CDLL:
         L.fyg_plan_destroy.argtypes = [vp]
         L.fyg_execute.argtypes = [vp, vp, vp, i, vp]
         L.fyg_execute_async.argtypes = [vp, vp, vp, i, vp]
+        L.fyg_plan_join.argtypes = [vp, vp]
+        L.fyg_device_signature.argtypes = [ctypes.c_char_p, sz]
         L.fyg_execute_adjoint.argtypes = [vp, vp, vp, d, vp]
         L.fyg_strategy.argtypes = [sz]
         L.fyg_gpu_strategy.argtypes = [sz]
@@ -141,6 +143,13 @@ def autotune_batch(lengths, dtype="complex64", cache_path: str | None = None) ->
     path = cache_path.encode() if cache_path else None
     check(lib().fyg_batch_autotune(arr, len(lens), code, path, ctypes.byref(ms)))
     return ms.value
+
+
+def device_signature() -> str:
+    """The current device's key in autotune caches: name|SMs|compute capability|driver."""
+    buf = ctypes.create_string_buffer(512)
+    check(lib().fyg_device_signature(buf, len(buf)))
+    return buf.value.decode()
 
 
 def plan_cache_stats() -> dict:
@@ -262,11 +271,15 @@ class FFT1D_C2C_invoker:
 
     def dispatch(self, invert: bool, input, output, stream=None, blocking: bool = True) -> None:
         """foye_FFT.hpp:128-151: dispatch<invert>(input, output).  blocking=False with host
-        buffers returns after enqueueing (fyg_execute_async): synchronize `stream` before
-        reading `output`."""
+        buffers returns after enqueueing (fyg_execute_async): call join(stream) and synchronize
+        `stream` (or the device) before reading `output`."""
         px, py = self._io(input, output)
         fn = lib().fyg_execute if blocking else lib().fyg_execute_async
         check(fn(self._h, px, py, FYG_INVERSE if invert else FYG_FORWARD, _stream_handle(stream)))
+
+    def join(self, stream=None) -> None:
+        """Make `stream` wait for the copy-outs of asynchronous host dispatches."""
+        check(lib().fyg_plan_join(self._h, _stream_handle(stream)))
 
     def forward(self, input, output, stream=None) -> None:
         self.dispatch(False, input, output, stream)

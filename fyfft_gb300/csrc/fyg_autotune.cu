@@ -224,6 +224,14 @@ int tune_store_key(const std::string& key, const TuneChoice& choice, const char*
 
 using namespace fyg;
 
+extern "C" int fyg_device_signature(char* buf, size_t len) {
+    if (!buf || len == 0) return set_error(FYG_ERR_NULL_PTR, "null buffer");
+    const std::string sig = device_signature();
+    if (sig.size() + 1 > len) return set_error(FYG_ERR_INVALID_ARG, "buffer too small");
+    std::memcpy(buf, sig.c_str(), sig.size() + 1);
+    return FYG_OK;
+}
+
 extern "C" int fyg_autotune(size_t n, int dtype, size_t batch, const char* cache_path, double* best_ms) {
     clear_error();
     if (n < 2 || batch < 1) return set_error(FYG_ERR_INVALID_ARG, "autotune: n >= 2 and batch >= 1");

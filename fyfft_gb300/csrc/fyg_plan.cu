@@ -1073,11 +1073,12 @@ static int ensure_staging(fyg_plan* pl) {
     return FYG_OK;
 }
 
-// async: return after enqueueing; the caller's stream reaches completion when the output is in
-// host memory, and the host input is read by the copy stream without waiting for earlier work
-// on the caller's stream (the caller has it ready), so consecutive calls of different plans
-// pipeline their copies and kernels.  Otherwise the copy-in waits for earlier work on the
-// caller's stream and the call returns when the output is in host memory.
+// async: return after enqueueing; the output is in host memory once the plan's copy-out stream
+// has finished (fyg_plan_join orders it into a caller stream), and the host input is read by the
+// copy stream without waiting for earlier work on the caller's stream (the caller has it
+// ready), so consecutive calls of different plans pipeline their copies and kernels.  Otherwise
+// the copy-in waits for earlier work on the caller's stream and the call returns when the output
+// is in host memory.
 // Asynchronous calls of one host thread on one device keep their copies in call order: each
 // call's first copy-in waits for the previous call's last copy-in, and likewise for copy-outs, so
 // the copy engines serve the transforms first in, first out (concurrent copy streams of many
@@ -1158,7 +1159,10 @@ static int execute_host_overlapped(fyg_plan* pl, const void* in, void* out, bool
         rc = chk(cudaEventRecord(chain->h2d, pl->s_h2d), "event");
         if (!rc) rc = chk(cudaEventRecord(chain->d2h, pl->s_d2h), "event");
     }
-    if (async && !rc) return chk(cudaStreamWaitEvent(st, pl->ev_out_free, 0), "wait");
+    // async: the copy-outs complete on the plan's copy-out stream (fyg_plan_join or a device
+    // synchronize waits for them); the caller's stream runs on, so the next call's kernels are
+    // not held behind this call's copies
+    if (async) return rc;
     // drain both copy streams before returning (the host buffers are the caller's)
     const cudaError_t e1 = cudaStreamSynchronize(pl->s_h2d);
     const cudaError_t e2 = cudaStreamSynchronize(pl->s_d2h);
@@ -1471,6 +1475,13 @@ int fyg_execute_async(fyg_plan* plan, const void* in, void* out, int direction, 
     if (direction != FYG_FORWARD && direction != FYG_INVERSE)
         return set_error(FYG_ERR_INVALID_ARG, "direction must be FYG_FORWARD or FYG_INVERSE");
     return execute_dir(plan, in, out, direction == FYG_INVERSE, 1.0, (cudaStream_t)stream, true);
+}
+
+int fyg_plan_join(fyg_plan* plan, void* stream) {
+    if (!plan) return set_error(FYG_ERR_NULL_PTR, "null plan");
+    if (!plan->ev_out_free) return FYG_OK;   // no asynchronous host execution yet
+    const cudaError_t e = cudaStreamWaitEvent((cudaStream_t)stream, plan->ev_out_free, 0);
+    return e == cudaSuccess ? FYG_OK : cuda_error(e, "join");
 }
 
 int fyg_execute_adjoint(fyg_plan* plan, const void* g, void* out, double scale, void* stream) {

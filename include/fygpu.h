@@ -96,6 +96,9 @@ int fyg_plan_create_ex(size_t n, int dtype, size_t batch, int flags, size_t max_
  * *best_ms (optional) receives the winner's time per forward batch. */
 int fyg_autotune(size_t n, int dtype, size_t batch, const char* cache_path, double* best_ms);
 
+/* The current device's key in autotune caches: "name|SM count|compute capability|driver". */
+int fyg_device_signature(char* buf, size_t len);
+
 /* Releases the plan and its device tables and scratch. */
 int fyg_plan_destroy(fyg_plan* plan);
 
@@ -117,13 +120,17 @@ int fyg_plan_cache_clear(void);
 int fyg_execute(fyg_plan* plan, const void* in, void* out, int direction, void* stream);
 
 /* As fyg_execute, but host buffers do not block: the call enqueues the staged copies and kernels
- * and returns; the output is in host memory once `stream` has completed (synchronize it before
- * reading `out` or reusing `in`).  The host input is read without waiting for earlier work on
- * `stream`, so it must be ready at the call; pinned host memory makes the copies asynchronous.
- * Consecutive calls of different plans then overlap one plan's copies with another's kernels.
- * Device buffers: identical to fyg_execute.  No counterpart in the reference (its dispatch is
- * synchronous). */
+ * and returns.  Large host batches copy out on the plan's own copy-out stream: the output is in
+ * host memory after fyg_plan_join(plan, s) and a synchronize of s (or a device synchronize);
+ * do not read `out` or reuse `in` before.  The host input is read without waiting for earlier
+ * work on `stream`, so it must be ready at the call; pinned host memory makes the copies
+ * asynchronous.  Consecutive calls of different plans overlap one plan's copies with another's
+ * kernels, and the copies of one host thread's calls run in call order.  Device buffers:
+ * identical to fyg_execute.  No counterpart in the reference (its dispatch is synchronous). */
 int fyg_execute_async(fyg_plan* plan, const void* in, void* out, int direction, void* stream);
+
+/* Makes `stream` wait for the copy-outs of the plan's asynchronous host executions. */
+int fyg_plan_join(fyg_plan* plan, void* stream);
 
 /* Adjoint (conjugate transpose) of the forward transform, times `scale`:
  * out = scale * F^H g = scale * N * dispatch<true>(g).  No counterpart in the reference; its

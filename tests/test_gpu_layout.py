@@ -108,6 +108,8 @@ def test_async_host_execution_pipelines_and_matches(n, batch):
         p1.dispatch(False, x1.numpy(), y1.numpy(), s, blocking=False)
         p2.dispatch(True, x2.numpy(), y2.numpy(), s, blocking=False)
         p1.dispatch(False, x1.numpy(), y1.numpy(), s, blocking=False)   # same plan again: staging reuse
+    p1.join(s)
+    p2.join(s)
     s.synchronize()
     r1, r2 = np.empty_like(x1.numpy()), np.empty_like(x2.numpy())
     p1.dispatch(False, x1.numpy(), r1)
