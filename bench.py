@@ -480,8 +480,17 @@ def uneven_batch(dev: int, stream, reps: int = 10, no_autotune: bool = False, ra
     t0 = time.perf_counter()
     tuned = None
     if not no_autotune:
-        # option sets of the persistent launch timed on this device, cached (FYG_AUTOTUNE_CACHE)
-        fg.autotune_batch(lengths, cache_path=os.environ.get("FYG_AUTOTUNE_CACHE"))
+        # execution forms and option sets timed on this device, cached (FYG_AUTOTUNE_CACHE);
+        # skipped when the cache already holds this length sequence for this device
+        cache = os.environ.get("FYG_AUTOTUNE_CACHE")
+        have = False
+        if cache and os.path.exists(cache):
+            with open(cache) as f:
+                doc = json.load(f)
+            have = doc.get("device") == fg.device_signature() and any(
+                k.startswith(f"batch32:{len(lengths)}:") for k in doc.get("entries", {}))
+        if not have:
+            fg.autotune_batch(lengths, cache_path=cache)
         tuned = round(time.perf_counter() - t0, 2)
     t1 = time.perf_counter()
     b = fg.UnevenBatch(lengths, flags=0 if no_autotune else fg.FYG_FLAG_AUTOTUNED)

@@ -194,7 +194,8 @@ int fyg_batch_autotune(const size_t* lengths, size_t count, int dtype, const cha
 /* fyg_batch_create with an explicit execution form (what the batch autotuner chooses between):
  * form 0: one persistent kernel over a device work queue (stage radix cap 16 or 32, single-pass
  * tiles up to single_tile_kb KB of shared memory; 0 = defaults); form 1: one plan per distinct
- * length (register-resident kernels where they apply) as parallel chains of one CUDA graph;
+ * length (register-resident kernels where they apply) as up to 32 parallel chains of one CUDA
+ * graph;
  * form 2: lengths up to `split` in the persistent kernel, longer ones as graph chains, both in
  * one graph.  FP64 batches always run form 1. */
 int fyg_batch_create_ex(const size_t* lengths, size_t count, int dtype, int flags, int form, size_t split,
