@@ -200,7 +200,8 @@ int build_persistent(fyg_batch* b) {
     for (auto& kv : b->group_plans) {
         const size_t len = kv.first;
         fyg_plan* pl = kv.second;
-        if (pl->strategy == GS_COPY || pl->chunk != pl->batch || pl->compute_bytes != 8) return FYG_ERR_UNSUPPORTED;
+        if (pl->strategy == GS_COPY || pl->strategy == GS_SPLIT || pl->chunk != pl->batch || pl->compute_bytes != 8)
+            return FYG_ERR_UNSUPPORTED;
         const std::vector<int>& mem = b->members[len];
         const int id0 = (int)ids.size();
         ids.insert(ids.end(), mem.begin(), mem.end());

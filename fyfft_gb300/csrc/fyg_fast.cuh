@@ -426,6 +426,7 @@ __global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1))
             // Rader: out[scatter[k]] = (x0 + y*scale (conjugated forward)) * scale2, and the DC
             // term out[0] = (x0 + A0) * scale2 with A0 the forward convolution's DC term
             float2* obase = reinterpret_cast<float2*>(p.out) + ci.out_base;
+            const int64_t os = p.split_m > 1 ? p.split_m : 1;
             const float2 x0 = ld_data(reinterpret_cast<const float2*>(p.x0buf) + ci.b);
             const float scale2 = (float)p.scale2;
             const int* scatter = p.scatter;
@@ -441,7 +442,7 @@ __global__ void __launch_bounds__(S::T, (S::T <= 384 ? 2 : 1))
                 if (t > 0) {
                     float2 u = cscale(v[i], scale);
                     if (p.conj_out) u.y = -u.y;
-                    obase[t] = cscale(cadd(x0, u), scale2);
+                    obase[t * os] = cscale(cadd(x0, u), scale2);
                 }
             }
         } else if (unit) {

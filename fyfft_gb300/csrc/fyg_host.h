@@ -72,6 +72,7 @@ enum GpuStrategy : int {
     GS_RADER = 2,       // Rader: cyclic (or zero-padded) convolution of length N-1
     GS_BLUESTEIN = 3,   // Bluestein chirp-z convolution
     GS_COPY = 4,        // n == 1
+    GS_SPLIT = 5,       // N = m p: length-m DFTs and twiddles, then m Rader transforms of length p
 };
 
 // Owned device allocation.
@@ -87,7 +88,8 @@ struct DevBuf {
 };
 
 // Buffer roles a pass reads from / writes to.
-enum Role : int { ROLE_IN = 0, ROLE_OUT = 1, ROLE_S0 = 2, ROLE_S1 = 3 };
+// ROLE_S2: the split strategy's buffer between its first pass and the Rader passes.
+enum Role : int { ROLE_IN = 0, ROLE_OUT = 1, ROLE_S0 = 2, ROLE_S1 = 3, ROLE_S2 = 4 };
 
 struct PassDesc {
     PassParams p;          // in/out/ncols/x0buf/dcbuf filled at execution
@@ -96,6 +98,8 @@ struct PassDesc {
     int threads;
     size_t smem;
     int64_t in_elem_bytes, out_elem_bytes;
+    int64_t in_len = 0, out_len = 0;   // elements per transform read / written
+    int bmul = 1;          // transforms of this pass per user transform (m for the split's Rader passes)
     bool tma = false;      // register-resident pass whose input arrives by TMA tile loads
     CUtensorMap tmap;      // (FYG_FLAG_TMA_LOADS; the input is a scratch buffer of the plan)
 };
@@ -124,7 +128,8 @@ struct fyg_plan {
     std::vector<fyg::PassDesc> fwd, inv;
     // device tables
     std::vector<std::shared_ptr<fyg::DevBuf>> tables;   // read-only, shared through the table cache
-    fyg::DevBuf scratch0, scratch1, x0buf, dcbuf, errword;
+    fyg::DevBuf scratch0, scratch1, scratch2, x0buf, dcbuf, errword;
+    size_t split_m = 1;       // GS_SPLIT: N = split_m * p
     fyg::DevBuf stage_in, stage_out;   // staging for host pointers
     size_t stage_in_bytes = 0;
     // host-pointer execution: copy-in and copy-out streams and per-chunk events, so that the

@@ -18,6 +18,8 @@ enum KernelVariant : int {
     KV_F64_OF32_C16,    // double compute, double in, float out
     KV_F64_F32IO_C16,   // double compute, float in,  float out
     KV_FAST,            // register-resident FP32 kernel of a power-of-two tile length (fyg_fast.cuh)
+    KV_SPLIT_F32,       // first pass of the N = m p split (fyg_split.cu), complex<float>
+    KV_SPLIT_F64,       // the same, complex<double>
     KV_COUNT
 };
 
@@ -27,6 +29,10 @@ VariantInfo variant_info(int kv);
 // Launches one tile pass; sets the dynamic shared-memory attribute when needed.
 cudaError_t launch_pass(int kv, const PassParams& p, unsigned grid, int threads, size_t smem,
                         cudaStream_t st, const CUtensorMap* tmap = nullptr);
+
+// First pass of the N = m p split: g.R = m, g.C = split_threads() columns per CTA.
+int split_threads();
+cudaError_t launch_split(int kv, const PassParams& p, unsigned grid, cudaStream_t st);
 
 // Register-resident kernels: the tile shape for R (false if R has none) and the launch.
 bool fast_shape(int R, int wide, int* C, int* threads, size_t* smem);

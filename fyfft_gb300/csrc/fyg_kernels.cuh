@@ -135,7 +135,7 @@ __device__ __forceinline__ Col<T> colmajor_col(const PassParams& p, int64_t q) {
     ci.k = 0;
     ci.out_j = 0;
     ci.in_base = ci.valid ? transform_base(p.in_offsets, p.ids, q, p.idist) : 0;
-    ci.out_base = ci.valid ? transform_base(p.out_offsets, p.ids, q, p.odist) : 0;
+    ci.out_base = ci.valid ? out_transform_base(p, q) : 0;
     ci.x0 = mk<cplx<T>>(T(0), T(0));
     return ci;
 }
@@ -299,6 +299,7 @@ __device__ __forceinline__ void store_general(const PassParams& p, const cplx<T>
     const T2* chirp = reinterpret_cast<const T2*>(p.chirp);
     const int* scatter = p.scatter;
     const T2* dcbuf = reinterpret_cast<const T2*>(p.dcbuf);
+    const int64_t ostride = p.split_m > 1 ? p.split_m : 1;
     const bool nfast = COLMAJOR || Ns_out == 1;
     const FastDiv divR = p.g.divR;
 #pragma unroll 4
@@ -330,7 +331,7 @@ __device__ __forceinline__ void store_general(const PassParams& p, const cplx<T>
             if (t > 0) {
                 u = cscale(u, scale);
                 if (conj_out) u = cconj(u);
-                gout[h.out_base + t] = to_c(cscale(cadd(h.x0, u), scale2), TO());
+                gout[h.out_base + t * ostride] = to_c(cscale(cadd(h.x0, u), scale2), TO());
             }
         }
     }

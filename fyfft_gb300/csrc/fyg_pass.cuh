@@ -110,10 +110,23 @@ struct alignas(16) PassParams {
     // w_R^(m k twm_s) at m ns_s + k (m < radix, k < ns_s), so that the lanes of a warp (consecutive
     // k for a fixed m) read consecutive entries
     const void* tw_stage;
+    // N = m p split (m > 1): transform b of this pass is sub-transform k1 = b mod m of user
+    // transform b / m, whose outputs sit at elements k1 + m k of that transform (Rader scatter
+    // store); 0 otherwise
+    int split_m;
 };
 
 __device__ __forceinline__ int64_t transform_base(const int64_t* offs, const int* ids, int64_t b, int64_t dist) {
     return offs ? offs[ids ? ids[b] : b] : b * dist;
+}
+
+// Output base of transform b of a pass (the N = m p split interleaves m sub-transforms).
+__device__ __forceinline__ int64_t out_transform_base(const PassParams& p, int64_t b) {
+    if (p.split_m > 1) {
+        const int64_t u = b / p.split_m;
+        return transform_base(p.out_offsets, p.ids, u, p.odist) + (b - u * p.split_m);
+    }
+    return transform_base(p.out_offsets, p.ids, b, p.odist);
 }
 
 // Data loads go through L2 only (ld.global.cg): every element is read once, and inside one
@@ -191,7 +204,7 @@ __device__ __forceinline__ Col<T> make_col(const PassParams& p, int64_t q) {
     const uint32_t qo = p.div_Ns_out.div(jj);
     ci.out_j = (int)(qo * (uint32_t)p.Ns_out * (uint32_t)p.g.R + (jj - qo * (uint32_t)p.Ns_out));
     ci.in_base = transform_base(p.in_offsets, p.ids, b, p.idist);
-    ci.out_base = transform_base(p.out_offsets, p.ids, b, p.odist);
+    ci.out_base = out_transform_base(p, b);
     ci.x0 = mk<T2>(T(0), T(0));
     return ci;
 }

@@ -43,12 +43,13 @@ cudaError_t launch_scale_copy(const void* in, void* out, size_t n, int dtype, do
                               cudaStream_t st);
 
 VariantInfo variant_info(int kv) {
-    return {512, (kv == KV_F32_C16 || kv == KV_F32_C32 || kv == KV_FAST) ? 8 : 16};
+    return {512, (kv == KV_F32_C16 || kv == KV_F32_C32 || kv == KV_FAST || kv == KV_SPLIT_F32) ? 8 : 16};
 }
 
 cudaError_t launch_pass(int kv, const PassParams& p, unsigned grid, int threads, size_t smem, cudaStream_t st,
                         const CUtensorMap* tmap) {
     if (kv == KV_FAST) return launch_fast(p, tmap, grid, st);
+    if (kv == KV_SPLIT_F32 || kv == KV_SPLIT_F64) return launch_split(kv, p, grid, st);
     if (kv == KV_F32_C16) return launch_f32(kv, p, grid, threads, smem, st);
     if (kv == KV_F32_C32) return launch_f32c32(kv, p, grid, threads, smem, st);
     if (kv == KV_F64_C16) return launch_f64(kv, p, grid, threads, smem, st);
@@ -217,6 +218,17 @@ static int ref_strategy(uint64_t n) {
     if (is_prime(n) && n <= 78125 && 2 * n - 3 <= 78125) return FYG_STRATEGY_RADER;
     if (n <= 39062) return FYG_STRATEGY_BLUESTEIN;
     return FYG_STRATEGY_DFT;
+}
+
+// N = m p with 2 <= m <= 8 and p prime, p - 1 13-smooth: m cyclic Rader transforms of length p
+// after one pass of length-m DFTs (fyg_split.cu) move about N points per pass, where a Bluestein
+// convolution moves 2N to 4N.  Returns m (0: no split) for lengths above 8192, whose Bluestein
+// convolution (length >= 2N - 1 > 16384) takes more than one pass.
+static uint64_t split_factor(uint64_t n) {
+    if (n <= 8192 || is_smooth(n, 13) || is_prime(n)) return 0;
+    for (uint64_t m = 2; m <= 8; ++m)
+        if (n % m == 0 && is_prime(n / m) && is_smooth(n / m - 1, 13)) return m;
+    return 0;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -481,6 +493,14 @@ struct PipeSpec {
     int threads = 0;          // single-pass: thread policy (single_pass_threads)
 };
 
+// The N = m p split: a first pass (fyg_split.cu) ahead of a Rader pipeline of length p over m
+// times the batch, whose scatter store interleaves the m transforms of each user transform.
+struct SplitSpec {
+    uint64_t m = 1;              // 1: no split
+    uint64_t p = 0;              // length of the Rader transforms
+    const void* tw = nullptr;    // w_N^t, t < N (user element type)
+};
+
 int pick_variant(int compute_cb, int tin_cb, int tout_cb, int cls) {
     if (compute_cb == 8) return cls <= 16 ? KV_F32_C16 : KV_F32_C32;
     if (tin_cb == 16 && tout_cb == 16) return KV_F64_C16;
@@ -530,7 +550,7 @@ bool single_pass_fits(int cb, uint64_t n, size_t cap) {
 
 static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
                           const std::map<int, const void*>& local_tabs, const void* tw_hi,
-                          const void* tw_lo, int tw_shift, const ConvTables& ct,
+                          const void* tw_lo, int tw_shift, const ConvTables& ct, const SplitSpec& sp,
                           std::vector<PassDesc>& out) {
     out.clear();
     const int P = (int)ps.prad.size();
@@ -608,12 +628,17 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
         p.gather = ct.gather;
         p.scatter = ct.scatter;
         p.err = reinterpret_cast<int*>(pl->errword.ptr);
-        d.in_role = first ? ROLE_IN : ((i - 1) % 2 == 0 ? ROLE_S0 : ROLE_S1);
+        const bool split = sp.m > 1;
+        d.in_role = first ? (split ? ROLE_S2 : ROLE_IN) : ((i - 1) % 2 == 0 ? ROLE_S0 : ROLE_S1);
         d.out_role = last ? ROLE_OUT : (i % 2 == 0 ? ROLE_S0 : ROLE_S1);
-        d.in_elem_bytes = d.in_role == ROLE_IN ? io_cb : cb;
+        d.in_elem_bytes = (d.in_role == ROLE_IN || d.in_role == ROLE_S2) ? io_cb : cb;
         d.out_elem_bytes = d.out_role == ROLE_OUT ? io_cb : cb;
-        p.idist = d.in_role == ROLE_IN ? (int64_t)pl->idist : (int64_t)L;
+        p.idist = d.in_role == ROLE_IN ? (int64_t)pl->idist : d.in_role == ROLE_S2 ? (int64_t)sp.p : (int64_t)L;
         p.odist = d.out_role == ROLE_OUT ? (int64_t)pl->odist : (int64_t)L;
+        d.in_len = d.in_role == ROLE_IN ? (int64_t)n : d.in_role == ROLE_S2 ? (int64_t)sp.p : (int64_t)L;
+        d.out_len = d.out_role == ROLE_OUT ? (int64_t)(split ? sp.p : n) : (int64_t)L;
+        d.bmul = (int)sp.m;
+        if (last && split) p.split_m = (int)sp.m;
         // load / store fusions
         p.load_mode = LD_PLAIN;
         p.store_mode = ST_PLAIN;
@@ -724,7 +749,7 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
         if (tma_wanted && d.kv == KV_FAST && p.load_mode == LD_PLAIN && p.Ns > 1 &&
             (d.in_role == ROLE_S0 || d.in_role == ROLE_S1) && (R % 256 == 0)) {
             const void* base = d.in_role == ROLE_S0 ? pl->scratch0.ptr : pl->scratch1.ptr;
-            if (encode_tile_map(&d.tmap, base, (uint64_t)p.Rr, (uint64_t)pl->chunk * (uint64_t)R, p.g.C, R) ==
+            if (encode_tile_map(&d.tmap, base, (uint64_t)p.Rr, (uint64_t)pl->chunk * sp.m * (uint64_t)R, p.g.C, R) ==
                 cudaSuccess)
                 d.tma = true;
             else
@@ -734,6 +759,30 @@ static int build_pipeline(fyg_plan* pl, const PipeSpec& ps, bool inverse,
             return set_error(FYG_ERR_UNSUPPORTED, "tile of " + std::to_string(R) + "x" + std::to_string(C) +
                                                       " exceeds shared memory");
         out.push_back(d);
+    }
+    if (sp.m > 1) {
+        // the split pass: user input -> scratch2 (m length-p transforms per user transform)
+        PassDesc d;
+        std::memset(&d.p, 0, sizeof(d.p));
+        PassParams& p = d.p;
+        p.g.R = (int)sp.m;
+        p.g.C = split_threads();
+        p.Rr = (int)sp.p;
+        p.div_Rr = make_fastdiv((uint32_t)sp.p);
+        p.idist = (int64_t)pl->idist;
+        p.odist = (int64_t)n;
+        p.conj_in = inverse ? 1 : 0;
+        p.tw_stage = sp.tw;
+        p.scale = p.scale2 = 1.0;
+        p.err = reinterpret_cast<int*>(pl->errword.ptr);
+        d.in_role = ROLE_IN;
+        d.out_role = ROLE_S2;
+        d.in_elem_bytes = d.out_elem_bytes = io_cb;
+        d.in_len = d.out_len = (int64_t)n;
+        d.kv = pl->dtype == FYG_C32 ? KV_SPLIT_F32 : KV_SPLIT_F64;
+        d.threads = split_threads();
+        d.smem = 0;
+        out.insert(out.begin(), d);
     }
     return FYG_OK;
 }
@@ -770,6 +819,8 @@ static int make_plan(fyg_plan* pl) {
         return FYG_OK;
     }
     // ---- strategy ----
+    // nt: length of the transforms the Rader / Bluestein passes compute (N / m for the split)
+    uint64_t nt = n, split_m = 1;
     const size_t single_cap = (pl->flags & FYG_FLAG_SMALL_TILES)
                                   ? (t_batch_single_cap ? std::min(t_batch_single_cap, kSmemLimit) : (100u << 10))
                                   : kSmemLimit;
@@ -789,7 +840,14 @@ static int make_plan(fyg_plan* pl) {
                 return set_error(FYG_ERR_INVALID_ARG, "Rader convolution length must be N-1 (13-smooth) or 7-smooth >= 2N-3");
             ps.L = t_conv_len;
         }
+    } else if (!t_conv_len && !(pl->flags & FYG_FLAG_SMALL_TILES) && (split_m = split_factor(n)) > 1) {
+        // N = m p: the first pass (fyg_split.cu) leaves m length-p transforms per transform,
+        // which run as a cyclic Rader pipeline over m times the batch
+        ps.kind = GS_RADER;
+        nt = n / split_m;
+        ps.L = nt - 1;
     } else {
+        split_m = 1;
         ps.kind = GS_BLUESTEIN;
         ps.L = next_smooth7(2 * n - 1);
         // FP32 multi-pass convolutions: the power-of-two length runs on the register-resident
@@ -805,7 +863,8 @@ static int make_plan(fyg_plan* pl) {
             ps.L = t_conv_len;
         }
     }
-    pl->strategy = ps.kind;
+    pl->strategy = split_m > 1 ? GS_SPLIT : ps.kind;
+    pl->split_m = split_m;
     pl->L = ps.L;
     const bool conv = ps.kind == GS_RADER || ps.kind == GS_BLUESTEIN;
     if (conv && pl->dtype == FYG_C32) {
@@ -834,7 +893,7 @@ static int make_plan(fyg_plan* pl) {
     }
     // ---- chunking: keep the scratch of one chunk L2-resident ----
     const int K = conv ? 2 * P - 1 : P;
-    if (K == 1) pl->chunk = pl->batch;
+    if (K == 1 && split_m == 1) pl->chunk = pl->batch;
     else {
         // Whole batch per pass unless a scratch buffer would exceed 4 GB: measured on GB300, an
         // L2-sized chunk (8-128 MB) is 1.1-1.5x slower than one launch per pass over the batch,
@@ -842,13 +901,14 @@ static int make_plan(fyg_plan* pl) {
         uint64_t chunk_mb = 4096;
         if (const char* e = std::getenv("FYG_CHUNK_MB")) chunk_mb = std::max<uint64_t>(1, std::strtoull(e, nullptr, 10));
         const uint64_t chunk_elems = (chunk_mb << 20) / cb;
-        uint64_t c = std::max<uint64_t>(1, chunk_elems / ps.L);
+        uint64_t c = std::max<uint64_t>(1, chunk_elems / (ps.L * split_m));
         if (pl->flags & FYG_FLAG_NO_L2_CHUNK) c = pl->batch;
         pl->chunk = (size_t)std::min<uint64_t>(c, pl->batch);
     }
     // column indices are 32-bit inside the kernels
     const uint64_t maxRr = ps.L / *std::min_element(ps.prad.begin(), ps.prad.end());
-    if ((uint64_t)pl->chunk * maxRr >= (1ull << 31) || ps.L >= (1ull << 31))
+    if ((uint64_t)pl->chunk * split_m * std::max<uint64_t>(maxRr, split_m > 1 ? nt : 1) >= (1ull << 31) ||
+        ps.L >= (1ull << 31))
         return set_error(FYG_ERR_INVALID_LENGTH, "length/batch too large for 32-bit tile indexing");
 
     int rc = pl->errword.alloc(16);
@@ -911,20 +971,20 @@ static int make_plan(fyg_plan* pl) {
         }, &ct.spectrum);
         if (rc) return rc;
     } else if (ps.kind == GS_RADER) {
-        const uint64_t Lc = n - 1, M = ps.L, g = primitive_root(n), ginv = powmod(g, n - 2, n);
+        const uint64_t Lc = nt - 1, M = ps.L, g = primitive_root(nt), ginv = powmod(g, nt - 2, nt);
         std::vector<uint64_t> gp(Lc);
         std::vector<int> gi(Lc);
         uint64_t cur = 1, curi = 1;
         for (uint64_t i = 0; i < Lc; ++i) {
             gp[i] = cur;
             gi[i] = (int)curi;
-            cur = mulmod(cur, g, n);
-            curi = mulmod(curi, ginv, n);
+            cur = mulmod(cur, g, nt);
+            curi = mulmod(curi, ginv, nt);
         }
-        ct.src_key = "R" + std::to_string(n) + ":" + std::to_string(M) + ":" + cbs;
+        ct.src_key = "R" + std::to_string(nt) + ":" + std::to_string(M) + ":" + cbs;
         // gather (M ints) then scatter (M ints)
         const void* maps = nullptr;
-        rc = cached_table(pl, "rader:" + std::to_string(n) + ":" + std::to_string(M), [&](DevBuf& b) {
+        rc = cached_table(pl, "rader:" + std::to_string(nt) + ":" + std::to_string(M), [&](DevBuf& b) {
             std::vector<int> gs(2 * M, -1);
             for (uint64_t i = 0; i < Lc; ++i) gs[i] = gi[i];
             int* scatter = gs.data() + M;
@@ -944,24 +1004,42 @@ static int make_plan(fyg_plan* pl) {
             std::vector<double2> kt(M, make_double2(0, 0));
             for (uint64_t m = 0; m < M; ++m) {
                 long double c, sn;
-                twiddle_ld(gp[m % Lc], n, &c, &sn);
+                twiddle_ld(gp[m % Lc], nt, &c, &sn);
                 kt[m] = make_double2((double)c, (double)sn);
             }
             return upload_spectrum(b, kt, cb);
         }, &ct.spectrum);
         if (rc) return rc;
-        rc = pl->x0buf.alloc(pl->chunk * cb);
-        if (!rc) rc = pl->dcbuf.alloc(pl->chunk * cb);
+        rc = pl->x0buf.alloc(pl->chunk * split_m * cb);
+        if (!rc) rc = pl->dcbuf.alloc(pl->chunk * split_m * cb);
         if (rc) return rc;
     }
     // ---- scratch ----
     if (K >= 2) {
-        rc = pl->scratch0.alloc(pl->chunk * ps.L * cb);
-        if (!rc && K >= 3) rc = pl->scratch1.alloc(pl->chunk * ps.L * cb);
+        rc = pl->scratch0.alloc(pl->chunk * split_m * ps.L * cb);
+        if (!rc && K >= 3) rc = pl->scratch1.alloc(pl->chunk * split_m * ps.L * cb);
         if (rc) return rc;
     }
-    rc = build_pipeline(pl, ps, false, local_tabs, tw_hi, tw_lo, tw_shift, ct, pl->fwd);
-    if (!rc) rc = build_pipeline(pl, ps, true, local_tabs, tw_hi, tw_lo, tw_shift, ct, pl->inv);
+    const void* split_tw = nullptr;
+    if (split_m > 1) {
+        // the split pass's output (user element type) and its table w_N^t, t < N
+        rc = pl->scratch2.alloc(pl->chunk * n * io_cb);
+        if (!rc)
+            rc = cached_table(pl, "splittw:" + std::to_string(n) + ":" + std::to_string(io_cb), [&](DevBuf& b) {
+                std::vector<unsigned char> t(n * io_cb);
+                for (uint64_t k = 0; k < n; ++k) {
+                    long double c, sn;
+                    twiddle_ld(k, n, &c, &sn);
+                    if (io_cb == 8) reinterpret_cast<float2*>(t.data())[k] = make_float2((float)c, (float)sn);
+                    else reinterpret_cast<double2*>(t.data())[k] = make_double2((double)c, (double)sn);
+                }
+                return b.upload(t.data(), t.size());
+            }, &split_tw);
+        if (rc) return rc;
+    }
+    const SplitSpec sp{split_m, nt, split_tw};
+    rc = build_pipeline(pl, ps, false, local_tabs, tw_hi, tw_lo, tw_shift, ct, sp, pl->fwd);
+    if (!rc) rc = build_pipeline(pl, ps, true, local_tabs, tw_hi, tw_lo, tw_shift, ct, sp, pl->inv);
     return rc;
 }
 
@@ -987,6 +1065,7 @@ static int run_pipeline(fyg_plan* pl, const std::vector<PassDesc>& pipe, const v
                     case ROLE_IN: return (void*)((const char*)in + c0 * pl->idist * io_cb);
                     case ROLE_OUT: return (void*)((char*)out + c0 * pl->odist * io_cb);
                     case ROLE_S0: return pl->scratch0.ptr;
+                    case ROLE_S2: return pl->scratch2.ptr;
                     default: return pl->scratch1.ptr;
                 }
             };
@@ -996,7 +1075,7 @@ static int run_pipeline(fyg_plan* pl, const std::vector<PassDesc>& pipe, const v
                 if (d.in_role == ROLE_IN) { p.in = in; p.in_offsets = offs; p.ids = ids; }
                 if (d.out_role == ROLE_OUT) { p.out = out; p.out_offsets = offs; p.ids = ids; }
             }
-            p.ncols = (int64_t)nb * p.Rr;
+            p.ncols = (int64_t)nb * d.bmul * p.Rr;
             p.x0buf = pl->x0buf.ptr;
             p.dcbuf = pl->dcbuf.ptr;
             if (i + 1 == pipe.size()) {
@@ -1407,7 +1486,7 @@ int fyg_plan_describe(const fyg_plan* plan, char* buf, size_t len) {
         char line[256];
         std::snprintf(line, sizeof(line),
                       "pass %zu: kernel=%s R=%d C=%d threads=%d smem=%zu Ns=%d Ns_out=%d load=%s%s store=%s%s\n", i,
-                      d.kv == KV_FAST ? "fast" : "generic", d.p.g.R, d.p.g.C, d.threads, d.smem, d.p.Ns, d.p.Ns_out,
+                      d.kv == KV_FAST ? "fast" : (d.kv == KV_SPLIT_F32 || d.kv == KV_SPLIT_F64) ? "split" : "generic", d.p.g.R, d.p.g.C, d.threads, d.smem, d.p.Ns, d.p.Ns_out,
                       kLoad[d.p.load_mode], d.p.Ns > 1 ? "+twiddle" : "", kStore[d.p.store_mode],
                       d.p.mid ? " mid" : "");
         s += line;
@@ -1445,19 +1524,14 @@ int fyg_plan_profile_read(fyg_plan* plan, double* total_ms, int64_t* launches, i
     }
     plan->prof_pending.clear();
     plan->prof_pool_used = 0;
-    const int io_cb = plan->dtype == FYG_C32 ? 8 : 16;
     for (int i = 0; i < np && i < max_passes; ++i) {
         const PassDesc& d = plan->fwd[i];
         // elements one launch reads and writes: a full sweep of the chunk's transforms, counted
         // at the length actually stored on each side (N for user buffers, L for scratch)
-        const int64_t nb = (int64_t)plan->chunk;
-        const int64_t rd = d.in_role == ROLE_IN ? (int64_t)plan->n : (int64_t)plan->L;
-        const int64_t wr = d.out_role == ROLE_OUT ? (int64_t)plan->n : (int64_t)plan->L;
+        const int64_t nb = (int64_t)plan->chunk * d.bmul;
         if (total_ms) total_ms[i] = plan->prof_ms[i];
         if (launches) launches[i] = plan->prof_launches[i];
-        if (bytes_per_launch)
-            bytes_per_launch[i] = nb * (rd * (d.in_role == ROLE_IN ? io_cb : plan->compute_bytes) +
-                                        wr * (d.out_role == ROLE_OUT ? io_cb : plan->compute_bytes));
+        if (bytes_per_launch) bytes_per_launch[i] = nb * (d.in_len * d.in_elem_bytes + d.out_len * d.out_elem_bytes);
     }
     if (n_passes) *n_passes = np;
     return FYG_OK;
@@ -1536,6 +1610,7 @@ int fyg_gpu_strategy(size_t n) {
     if (is_smooth(n, 7)) return ref_directly_supported(n) ? FYG_STRATEGY_KERNEL_DIRECT : FYG_STRATEGY_MIX_RADIX;
     if (is_smooth(n, 13)) return FYG_STRATEGY_MIX_RADIX;
     if (is_prime(n) && (is_smooth(n - 1, 13) || 2 * n - 3 <= 78125)) return FYG_STRATEGY_RADER;
+    if (split_factor(n)) return FYG_STRATEGY_RADER;   // m Rader transforms after the split pass
     return FYG_STRATEGY_BLUESTEIN;
 }
 

@@ -63,7 +63,8 @@ def test_autotuned_convolution_length_is_used(cache):
         tuned = fg.FFT1D_C2C_invoker(n, "complex64", 1, flags=fg.FYG_FLAG_AUTOTUNED).info()["conv_length"]
         default = fg.FFT1D_C2C_invoker(n, "complex64", 1).info()["conv_length"]
         assert tuned == (m if m else default)
-        assert tuned == n - 1 or tuned >= 2 * n - 3
+        # Rader of N, Rader of p for the split N = 2 p (131074 = 2 x 65537), or Bluestein
+        assert tuned in (n - 1, n // 2 - 1) or tuned >= 2 * n - 3
 
 
 @pytest.mark.parametrize("n,m", [(999983, 2000000), (999983, 2016000), (131074, 263424), (65537, 131220)])
