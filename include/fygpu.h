@@ -144,8 +144,10 @@ int fyg_strategy(size_t n);
 /* Strategy this library runs for n (never FYG_STRATEGY_DFT). */
 int fyg_gpu_strategy(size_t n);
 
-/* Plan introspection: algorithm length (conv length M for Rader/Bluestein), number of kernel
- * passes per direction, and the GPU strategy. */
+/* Plan introspection: algorithm length (conv length M for Rader/Bluestein, p - 1 for the
+ * N = m p split), number of kernel passes per direction, and the GPU strategy (0 single pass,
+ * 1 multi-pass, 2 Rader, 3 Bluestein, 4 copy for N = 1, 5 the N = m p split: a pass of
+ * length-m DFTs ahead of m Rader transforms of the prime p). */
 int fyg_plan_info(const fyg_plan* plan, size_t* conv_length, int* passes, int* strategy);
 
 /* Device-side error bits the plan's kernels recorded since the last call (synchronizes the

@@ -55,6 +55,17 @@ def test_gpu_strategy_never_dft():
     assert L.fyg_gpu_strategy(1009) == 2 and L.fyg_gpu_strategy(2520) == 1
 
 
+def test_split_lengths_report_rader():
+    """N = m p (m <= 8, p prime with p - 1 13-smooth, N > 8192) runs m Rader transforms; other
+    composites stay Bluestein."""
+    L = fg.lib()
+    for n in (131074, 196611, 24578, 73734, 98312, 53767, 17285, 13828):
+        assert L.fyg_gpu_strategy(n) == 2, n
+    # 131078 = 2 x 65539 (65538 not 13-smooth), 6914 = 2 x 3457 (<= 8192), 9 x 12289 (m > 8)
+    for n in (131078, 6914, 9 * 12289):
+        assert L.fyg_gpu_strategy(n) == 3, n
+
+
 def test_generator_is_counter_based_and_distributed():
     a = fg.fill_random(5, 1 << 18, np.complex64, "uniform")
     b = fg.fill_random(5, 1 << 10, np.complex64, "uniform")
