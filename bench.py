@@ -380,7 +380,7 @@ def dominant_pass(plans_items, total_ms, hbm_peak):
     if not best:
         return None
     tms, nl, bpl, n, i, npass, pdesc = best
-    kind = "k_fast" if "kernel=fast" in pdesc else "k_pass"
+    kind = "k_fast" if "kernel=fast" in pdesc else "k_split" if "kernel=split" in pdesc else "k_pass"
     shape = " ".join(w for w in pdesc.split() if w.startswith(("R=", "C=")))
     avg_ms = tms / nl
     achieved = bpl / (avg_ms * 1e-3) / 1e9
