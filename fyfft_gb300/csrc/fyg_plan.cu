@@ -1180,7 +1180,7 @@ static int execute_host_overlapped(fyg_plan* pl, const void* in, void* out, bool
     // call whatever its size, and 9.3-10.1 ms with 16-32 chunks.
     size_t want = 16, chunk_mb = 64;
     if (const char* e = std::getenv("FYG_HOST_CHUNKS")) want = std::max<size_t>(1, std::strtoull(e, nullptr, 10));
-    if (const char* e = std::getenv("FYG_HOST_CHUNK_MB")) chunk_mb = std::strtoull(e, nullptr, 10);
+    if (const char* e = std::getenv("FYG_HOST_CHUNK_MB")) chunk_mb = std::min<size_t>(std::strtoull(e, nullptr, 10), 1u << 20);
     if (chunk_mb) {
         const size_t bytes = pl->n * pl->batch * (pl->dtype == FYG_C32 ? 8 : 16);
         want = std::min(want, std::max<size_t>(2, (bytes + (chunk_mb << 20) - 1) / (chunk_mb << 20)));
