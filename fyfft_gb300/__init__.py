@@ -45,6 +45,7 @@ EXPORTED_SYMBOLS = (
     "fyg_partition", "fyg_multi_create", "fyg_multi_shards", "fyg_multi_execute", "fyg_multi_execute_device",
     "fyg_multi_synchronize", "fyg_multi_destroy", "fyg_fill_random_at", "fyg_fill_random_device_at",
     "fyg_plan_status", "fyg_execute_async", "fyg_batch_create_ex", "fyg_plan_join", "fyg_device_signature",
+    "fyg_plan_schedule",
 )
 
 
@@ -87,6 +88,8 @@ def lib() -> ctypes.CDLL:
         L.fyg_strategy.argtypes = [sz]
         L.fyg_gpu_strategy.argtypes = [sz]
         L.fyg_plan_info.argtypes = [vp, ctypes.POINTER(sz), ctypes.POINTER(i), ctypes.POINTER(i)]
+        L.fyg_plan_schedule.argtypes = [sz, i, i, ctypes.POINTER(i), ctypes.POINTER(sz), ctypes.POINTER(i),
+                                        ctypes.POINTER(i), i, ctypes.POINTER(i)]
         L.fyg_plan_launches.argtypes = [vp, ctypes.POINTER(i)]
         L.fyg_plan_describe.argtypes = [vp, ctypes.c_char_p, sz]
         L.fyg_plan_profile.argtypes = [vp, i]
@@ -157,6 +160,19 @@ def plan_cache_stats() -> dict:
     e, b, h, m = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_uint64(), ctypes.c_uint64()
     check(lib().fyg_plan_cache_stats(ctypes.byref(e), ctypes.byref(b), ctypes.byref(h), ctypes.byref(m)))
     return {"entries": e.value, "bytes": b.value, "hits": h.value, "misses": m.value}
+
+
+def plan_schedule(length: int, dtype="complex64", flags: int = 0) -> dict:
+    """The schedule a plan of `length` gets, computed on the host (no GPU needed): GPU strategy
+    (as FFT1D_C2C_invoker.info() reports it), algorithm length L, split factor m and the pass
+    radices of the length-L transform."""
+    code = {"complex64": 0, "complex128": 1}[str(np.dtype(dtype))]
+    st, L, m, npass = ctypes.c_int(), ctypes.c_size_t(), ctypes.c_int(), ctypes.c_int()
+    rad = (ctypes.c_int * 16)()
+    check(lib().fyg_plan_schedule(int(length), code, int(flags), ctypes.byref(st), ctypes.byref(L), ctypes.byref(m),
+                                  rad, 16, ctypes.byref(npass)))
+    return {"gpu_strategy": st.value, "conv_length": L.value, "split_m": m.value,
+            "pass_radices": list(rad[:min(npass.value, 16)])}
 
 
 def plan_cache_clear() -> None:

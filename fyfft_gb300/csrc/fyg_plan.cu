@@ -29,6 +29,7 @@
 #include <cstring>
 #include <functional>
 #include <map>
+#include <memory>
 #include <mutex>
 
 #include "fyg_host.h"
@@ -805,22 +806,17 @@ static int upload_spectrum(DevBuf& b, const std::vector<double2>& kernel_time, i
     return b.upload(H.data(), M * sizeof(double2));
 }
 
-static int make_plan(fyg_plan* pl) {
+// The schedule of a plan, without touching the GPU: strategy, algorithm length, the N = m p
+// split factor, pass radices, and for single-pass lengths the transforms per CTA.  Sets
+// pl->strategy, split_m, L, conv_fp64 and compute_bytes from pl->n, dtype, flags and batch (and
+// the schedule options of plan_create_opts).  n >= 2.
+static int plan_spec(fyg_plan* pl, PipeSpec& ps, uint64_t& nt, uint64_t& split_m) {
     const uint64_t n = pl->n;
     const int io_cb = pl->dtype == FYG_C32 ? 8 : 16;
-    PipeSpec ps;
     ps.C = 1;
-    ConvTables ct;
-
-    if (n == 1) {
-        pl->strategy = GS_COPY;
-        pl->L = 1;
-        pl->compute_bytes = io_cb;
-        return FYG_OK;
-    }
-    // ---- strategy ----
     // nt: length of the transforms the Rader / Bluestein passes compute (N / m for the split)
-    uint64_t nt = n, split_m = 1;
+    nt = n;
+    split_m = 1;
     const size_t single_cap = (pl->flags & FYG_FLAG_SMALL_TILES)
                                   ? (t_batch_single_cap ? std::min(t_batch_single_cap, kSmemLimit) : (100u << 10))
                                   : kSmemLimit;
@@ -886,11 +882,33 @@ static int make_plan(fyg_plan* pl) {
                     return set_error(FYG_ERR_UNSUPPORTED, "reversed pass order does not fit shared memory");
         }
     }
-    const int P = (int)ps.prad.size();
-    if (P == 1) {
+    if (ps.prad.size() == 1) {
         ps.C = single_pass_cols(cb, (int)ps.L, pl->batch, t_cols);
         ps.threads = t_threads;
     }
+    return FYG_OK;
+}
+
+static int make_plan(fyg_plan* pl) {
+    const uint64_t n = pl->n;
+    const int io_cb = pl->dtype == FYG_C32 ? 8 : 16;
+    PipeSpec ps;
+    ps.C = 1;
+    ConvTables ct;
+
+    if (n == 1) {
+        pl->strategy = GS_COPY;
+        pl->L = 1;
+        pl->compute_bytes = io_cb;
+        return FYG_OK;
+    }
+    // ---- strategy and pass schedule ----
+    uint64_t nt = n, split_m = 1;
+    int rc = plan_spec(pl, ps, nt, split_m);
+    if (rc) return rc;
+    const bool conv = ps.kind == GS_RADER || ps.kind == GS_BLUESTEIN;
+    const int cb = pl->compute_bytes;
+    const int P = (int)ps.prad.size();
     // ---- chunking: keep the scratch of one chunk L2-resident ----
     const int K = conv ? 2 * P - 1 : P;
     if (K == 1 && split_m == 1) pl->chunk = pl->batch;
@@ -911,7 +929,7 @@ static int make_plan(fyg_plan* pl) {
         ps.L >= (1ull << 31))
         return set_error(FYG_ERR_INVALID_LENGTH, "length/batch too large for 32-bit tile indexing");
 
-    int rc = pl->errword.alloc(16);
+    rc = pl->errword.alloc(16);
     if (rc) return rc;
     cudaMemset(pl->errword.ptr, 0, 16);
     // ---- tables ----
@@ -1623,6 +1641,43 @@ int fyg_gpu_strategy(size_t n) {
     if (is_prime(n) && (is_smooth(n - 1, 13) || 2 * n - 3 <= 78125)) return FYG_STRATEGY_RADER;
     if (split_factor(n)) return FYG_STRATEGY_RADER;   // m Rader transforms after the split pass
     return FYG_STRATEGY_BLUESTEIN;
+}
+
+int fyg_plan_schedule(size_t n, int dtype, int flags, int* strategy, size_t* conv_length, int* split_m,
+                      int* pass_radices, int max_passes, int* npasses) {
+    clear_error();
+    if (n < 1) return set_error(FYG_ERR_INVALID_LENGTH, "length must be >= 1");
+    if (dtype != FYG_C32 && dtype != FYG_C64) return set_error(FYG_ERR_INVALID_ARG, "dtype must be FYG_C32 or FYG_C64");
+    if (n >= (1ull << 31)) return set_error(FYG_ERR_INVALID_LENGTH, "length must be < 2^31");
+    // a host-only plan object: plan_spec allocates nothing and makes no CUDA call
+    auto pl = std::make_unique<fyg_plan>();
+    pl->n = n;
+    pl->batch = 1;
+    pl->idist = pl->odist = n;
+    pl->dtype = dtype;
+    pl->flags = flags & ~FYG_FLAG_AUTOTUNED;
+    int st = GS_COPY;
+    size_t L = 1;
+    uint64_t m = 1;
+    std::vector<int> rad;
+    if (n >= 2) {
+        PipeSpec ps;
+        uint64_t nt = n;
+        t_radix_cap = (pl->flags & FYG_FLAG_SMALL_TILES) ? (t_batch_radix_cap ? t_batch_radix_cap : 16) : 0;
+        const int rc = plan_spec(pl.get(), ps, nt, m);
+        t_radix_cap = 0;
+        if (rc) return rc;
+        st = pl->strategy;
+        L = ps.L;
+        rad = ps.prad;
+    }
+    if (strategy) *strategy = st;
+    if (conv_length) *conv_length = L;
+    if (split_m) *split_m = (int)m;
+    if (pass_radices)
+        for (int i = 0; i < (int)rad.size() && i < max_passes; ++i) pass_radices[i] = rad[i];
+    if (npasses) *npasses = (int)rad.size();
+    return FYG_OK;
 }
 
 int fyg_plan_info(const fyg_plan* plan, size_t* conv_length, int* passes, int* strategy) {

@@ -150,6 +150,16 @@ int fyg_gpu_strategy(size_t n);
  * length-m DFTs ahead of m Rader transforms of the prime p). */
 int fyg_plan_info(const fyg_plan* plan, size_t* conv_length, int* passes, int* strategy);
 
+/* The schedule fyg_plan_create chooses for n with these flags, computed on the host (no GPU
+ * needed; FYG_FLAG_AUTOTUNED is ignored): the strategy (numbered as fyg_plan_info reports it),
+ * the algorithm length L (n, the convolution length, or p - 1 for the N = m p split), the split
+ * factor m (1 when there is none) and the radices of the passes of the length-L transform (up
+ * to max_passes written; the pass count in *npasses).  A Rader or Bluestein plan runs 2P - 1
+ * kernels for P passes (the last forward and the first inverse pass share one), the split one
+ * more.  Any output pointer may be NULL. */
+int fyg_plan_schedule(size_t n, int dtype, int flags, int* strategy, size_t* conv_length, int* split_m,
+                      int* pass_radices, int max_passes, int* npasses);
+
 /* Device-side error bits the plan's kernels recorded since the last call (synchronizes the
  * stream, then clears them): 1 = a stage radix the kernel was not compiled for, 4 = a TMA tile
  * load that did not complete within its bounded wait.  0 = no error.  Kernels record such
