@@ -1180,6 +1180,9 @@ static int ensure_staging(fyg_plan* pl) {
 // call's first copy-in waits for the previous call's last copy-in, and likewise for copy-outs, so
 // the copy engines serve the transforms first in, first out (concurrent copy streams of many
 // plans were measured to slow the first transforms and with them the whole pipeline).
+// The two events of a (host thread, device) pair live as long as the thread: they are created on
+// its first asynchronous call and deliberately not destroyed at thread exit, when the CUDA
+// context may already be gone (two events per thread and device).
 namespace {
 struct CopyChain {
     cudaEvent_t h2d = nullptr, d2h = nullptr;
