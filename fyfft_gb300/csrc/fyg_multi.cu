@@ -33,6 +33,8 @@ struct fyg_multi {
     std::vector<fyg_plan*> plans;        // one per shard (null for an empty shard)
     std::vector<cudaStream_t> streams;   // one per shard, on the shard's device
     ~fyg_multi() {
+        int prev = 0;
+        cudaGetDevice(&prev);
         for (size_t i = 0; i < plans.size(); ++i) {
             if (streams[i]) {
                 cudaSetDevice(devices[i]);
@@ -40,6 +42,7 @@ struct fyg_multi {
             }
             fyg_plan_destroy(plans[i]);
         }
+        cudaSetDevice(prev);   // the caller's device, as every other entry point leaves it
     }
 };
 

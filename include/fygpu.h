@@ -215,7 +215,9 @@ int fyg_batch_create_ex(const size_t* lengths, size_t count, int dtype, int flag
 int fyg_batch_destroy(fyg_batch* batch);
 
 /* offsets_dev: device array of `count` int64 element offsets (NULL: packed back to back in the
- * order given).  in/out device pointers. */
+ * order given).  in/out device pointers.  The work is a CUDA graph captured on the first call
+ * with each (direction, in, out, offsets_dev) and replayed on later calls with the same four;
+ * the batch keeps every graph it captured until fyg_batch_destroy. */
 int fyg_batch_execute(fyg_batch* batch, const void* in, void* out, const int64_t* offsets_dev,
                       int direction, void* stream);
 
