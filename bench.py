@@ -644,7 +644,7 @@ def cpu_baseline(items, args, check=None, uneven=None):
                "per_size_gflops": r["per_size_gflops"]}
     if check is not None:
         plans, youts = check
-        vs_ref, vs_oracle = {}, {}
+        vs_ref, vs_oracle, max_abs = {}, {}, {}
         threads = os.cpu_count() or 1
         for (n, batch, dt, dist, seed), y in zip(items, youts):
             g = y.view(batch, n)
@@ -652,12 +652,16 @@ def cpu_baseline(items, args, check=None, uneven=None):
             gr = g[rows].cpu().numpy()
             x = O.fill_random(seed, n * batch, np.complex128 if dt == "complex128" else np.complex64,
                               dist).reshape(batch, n)
-            vs_oracle[str(n)] = float(f"{O.rel_l2(gr, O.fft_batch(x[rows].astype(np.complex128), threads=threads)):.3e}")
+            ref = O.fft_batch(x[rows].astype(np.complex128), threads=threads)
+            vs_oracle[str(n)] = float(f"{O.rel_l2(gr, ref):.3e}")
+            max_abs[str(n)] = float(f"{np.max(np.abs(gr.astype(np.complex128) - ref)):.3e}")
             if "outputs" in r and n in r["outputs"]:
                 vs_ref[str(n)] = float(f"{O.rel_l2(g.cpu().numpy(), r['outputs'][n]):.3e}")
         res["gpu_rel_l2_vs_reference"] = vs_ref
         res["gpu_rel_l2_vs_fp64_oracle"] = vs_oracle
-        res["rel_l2_rows"] = "vs reference: whole batch; vs FP64 oracle: first and last transform"
+        res["gpu_max_abs_vs_fp64_oracle"] = max_abs
+        res["rel_l2_rows"] = ("vs reference: whole batch; vs FP64 oracle (rel-L2 and max abs): first and last "
+                              "transform")
     if uneven is not None:
         import concurrent.futures as cf
         lengths, xh, yh = uneven

@@ -1,11 +1,13 @@
-"""bench.py's reference arm on the CPU (no GPU involved): the reference's own FFT over the lengths
-it runs, one JSON line with the keys of the benchmark contract, lengths it cannot run listed
-with the reason, and ranks above 0 printing nothing."""
+"""bench.py on the CPU (no GPU involved).  The reference arm: the reference's own FFT over the
+lengths it runs, one JSON line with the keys of the benchmark contract, lengths it cannot run
+listed with the reason, and ranks above 0 printing nothing.  The CPU-baseline report: rel-L2 and
+max-abs errors of given outputs against the reference and the FP64 oracle."""
 import json
 import os
 import subprocess
 import sys
 
+import numpy as np
 import pytest
 
 from oracle import oracle as O
@@ -47,3 +49,26 @@ def test_reference_arm_runs_on_rank_zero_only():
 def test_reference_arm_reports_a_workload_it_cannot_run():
     lines = run_bench("--impl", "reference", "--steps", "3", "--warmup", "3", "--sizes", "65537")
     assert lines == [{"impl": "reference", "unavailable": "the reference can run none of this workload's lengths"}]
+
+
+def test_cpu_baseline_reports_errors_against_reference_and_oracle():
+    """The benchmark's error report on outputs held in CPU tensors: here the oracle's own FP64
+    results rounded to complex<float>, so every error is at FP32 rounding level."""
+    torch = pytest.importorskip("torch")
+    sys.path.insert(0, ROOT)
+    import bench
+    items = [(2520, 4, "complex64", "normal", 1), (1009, 3, "complex64", "normal", 1),
+             (65537, 2, "complex64", "normal", 1)]
+    youts = []
+    for n, b, _, dist, seed in items:
+        x = O.fill_random(seed, n * b, np.complex64, dist).reshape(b, n)
+        youts.append(torch.from_numpy(O.fft_batch(x.astype(np.complex128)).astype(np.complex64).reshape(-1)))
+    res = bench.cpu_baseline(items, None, check=(None, youts))
+    assert res["kind"] == "reference" and res["value"] > 0
+    assert set(res["gpu_rel_l2_vs_fp64_oracle"]) == {"2520", "1009", "65537"}
+    assert set(res["gpu_rel_l2_vs_reference"]) == {"2520", "1009"}          # 65537: not runnable there
+    for n, e in res["gpu_rel_l2_vs_fp64_oracle"].items():
+        assert e <= 1e-7, (n, e)
+        assert 0 < res["gpu_max_abs_vs_fp64_oracle"][n] <= 1e-4 * np.sqrt(int(n)), n
+    for n, e in res["gpu_rel_l2_vs_reference"].items():
+        assert e <= 4 * np.log2(int(n)) * float(np.finfo(np.float32).eps), (n, e)
