@@ -568,7 +568,7 @@ def reference_handle():
     return O.Reference(), None
 
 
-def reference_steps(items, steps: int, warmup: int, budget_s: float = 150.0):
+def reference_steps(items, steps: int, warmup: int, budget_s: float = 150.0, threads: int | None = None):
     """Times the reference's FFT1D_C2C_invoker over every item it can run, the whole batch per
     step, one plan per host thread (oracle/ref/ref_capi.cpp pools).  Inputs come from the
     oracle's restatement of the seeded generator, never from the GPU library.  Returns a dict
@@ -577,7 +577,7 @@ def reference_steps(items, steps: int, warmup: int, budget_s: float = 150.0):
     ref, why = reference_handle()
     if ref is None:
         return {"unavailable": why}
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     run, unsupported, pools, bufs = [], {}, [], []
     plan_s = 0.0
     for (n, batch, dt, dist, seed) in items:
@@ -641,7 +641,13 @@ def cpu_baseline(items, args, check=None, uneven=None):
                           f"({', '.join(f'{b}x{n}' for n, b in r['run'])}), one plan per thread; "
                           f"unsupported: {', '.join(r['unsupported']) or 'none'}"),
                "seconds": round(r["seconds"], 2), "plan_s": round(r["plan_s"], 2),
-               "per_size_gflops": r["per_size_gflops"]}
+               "per_size_gflops": r["per_size_gflops"], "machine": os.uname().machine, "cpu": r["cpu"]}
+        # the same code on one thread (the reference itself is single-threaded; the value above
+        # spreads the batch over every core, one plan per thread)
+        r1 = reference_steps(items, steps=1, warmup=1, budget_s=15.0, threads=1)
+        if "unavailable" not in r1:
+            res["single_thread"] = {"value": round(r1["value"], 3), "unit": "GFLOP/s", "cores": 1,
+                                    "steps": r1["steps"], "seconds": round(r1["seconds"], 2)}
     if check is not None:
         plans, youts = check
         vs_ref, vs_oracle, max_abs = {}, {}, {}

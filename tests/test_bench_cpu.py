@@ -64,7 +64,8 @@ def test_cpu_baseline_reports_errors_against_reference_and_oracle():
         x = O.fill_random(seed, n * b, np.complex64, dist).reshape(b, n)
         youts.append(torch.from_numpy(O.fft_batch(x.astype(np.complex128)).astype(np.complex64).reshape(-1)))
     res = bench.cpu_baseline(items, None, check=(None, youts))
-    assert res["kind"] == "reference" and res["value"] > 0
+    assert res["kind"] == "reference" and res["value"] > 0 and res["machine"]
+    assert res["single_thread"]["cores"] == 1 and res["single_thread"]["value"] > 0
     assert set(res["gpu_rel_l2_vs_fp64_oracle"]) == {"2520", "1009", "65537"}
     assert set(res["gpu_rel_l2_vs_reference"]) == {"2520", "1009"}          # 65537: not runnable there
     for n, e in res["gpu_rel_l2_vs_fp64_oracle"].items():
