@@ -14,7 +14,8 @@
 // (n * batch * element size, twice that for three or more passes) and twiddle tables of at most
 // kNoAllocTableBytes; device pointers of the current device only.  The first call on a device
 // sets up: it looks up the array's device address with cudaGetSymbolAddress and copies this
-// file's codelet constants (both synchronous host calls, no allocation).  The twiddle tables
+// file's codelet constants (both synchronous host calls, no allocation), so that first call
+// should come before any stream capture.  The twiddle tables
 // are computed on the device by a small kernel into the array (no host copy) whenever the
 // length or the element type differs from the previous call's on that device.  All calls
 // share the array and it keeps the last call's contents: two calls that overlap on the GPU
